@@ -1,0 +1,454 @@
+#!/usr/bin/env python3
+"""Benchmark: tce_sort_4 sweep effective GB/s on one GB300 (and replicas).
+
+Workload (one "step"): the tce_sort_4 sweep -- all 24 permutations of a rank-4
+FP64 tensor at dims 20^4, 30^4, 50^4, 100^4 (800 MB per tensor) and
+(17,29,64,100), factors {1.0, -1.0, 0.5}, sort and sortacc: 720 launches.
+Inputs are seeded uniform(-1,1) FP64 resident in HBM.  Each launch is timed
+with CUDA events on its stream; before every launch whose tensors are smaller
+than 2x L2 (129 MB) the L2 is flushed by writing a 512 MB scratch buffer
+outside the timed events.  value = algorithmic bytes (16 B/element for sort,
+24 B/element for sortacc) / summed kernel time.
+
+e2e: the same sweep through the reference-facing C ABI (tce_sort_4 /
+tce_sortacc_4) with pinned HOST buffers, wall-clocked per call: each call
+copies its input (and, for sortacc, its output) host->device, runs the
+kernel, and copies the output back.
+
+--impl reference: the reference's own C loop nests (generated by
+trunk/generator2.py, built by oracle/make_ref.py with OpenMP over every host
+core), best of the 24 loop orders per permutation tuned at 30^4, timed over a
+bounded per-step sample of the same sweep.
+
+Multi-GPU: the sweep has no exchange step, so N ranks run N independent
+replicas ("replicas only"); value = all ranks' bytes / max rank time.
+"""
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sort4 sweep effective GB/s (24 perms x {20^4,30^4,50^4,100^4,17x29x64x100} x f{1,-1,0.5} x {sort,sortacc}), FP64"
+UNIT = "GB/s"
+L2_BYTES = 129 * 1024 * 1024
+WORKLOAD = ("tce_sort_4 sweep: 24 perms x dims {20^4, 30^4, 50^4, 100^4, (17,29,64,100)} "
+            "x f in {1.0,-1.0,0.5} x {sort, sortacc}, FP64 uniform(-1,1)")
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sms, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+def sweep_cases():
+    from spaghetty_gb300.workloads import PERMS4, SORT4_DIMS, SORT4_FACTORS
+    cases = []
+    for dims in SORT4_DIMS:
+        for perm in PERMS4:
+            for f in SORT4_FACTORS:
+                for acc in (False, True):
+                    cases.append((dims, perm, f, acc))
+    return cases
+
+
+def case_bytes(dims, acc):
+    n = 1
+    for d in dims:
+        n *= d
+    return n * (24 if acc else 16)
+
+
+def traffic_from_profile():
+    """dram bytes per launch of the dominant kernel, from the committed ncu
+    summary (profiles/tiled_sort4_100.md, line 'traffic_bytes_per_launch: X')."""
+    path = os.path.join(ROOT, "profiles", "tiled_sort4_100.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except Exception:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, ws, rank, local):
+    import torch
+    import spaghetty_gb300 as S
+    from spaghetty_gb300._lib import lib, int_array
+    import ctypes
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    L = lib()
+    cases = sweep_cases()
+    sizes = sorted({c[0] for c in cases}, key=lambda d: -int(torch.tensor(d).prod()))
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(1234 + rank)
+    bufs = {}
+    for dims in sizes:
+        n = 1
+        for d in dims:
+            n *= d
+        u = torch.rand(n, dtype=torch.float64, device=dev, generator=gen) * 2 - 1
+        s = torch.rand(n, dtype=torch.float64, device=dev, generator=gen) * 2 - 1
+        bufs[dims] = (u, s, n)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def launch(dims, perm, f, acc):
+        u, s, n = bufs[dims]
+        rc = L.spaghetty_sort_async(4, ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(s.data_ptr()),
+                                    int_array(dims), int_array(perm), f, 1.0 if acc else 0.0, sp)
+        if rc:
+            raise RuntimeError("spaghetty_sort_async failed: %d" % rc)
+
+    def one_step(record):
+        evs = []
+        for (dims, perm, f, acc) in cases:
+            n = bufs[dims][2]
+            if n * 8 * 2 < 2 * L2_BYTES:
+                flush.fill_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            launch(dims, perm, f, acc)
+            e1.record(stream)
+            evs.append((dims, perm, f, acc, e0, e1))
+        if record:
+            return evs
+        return None
+
+    for _ in range(args.warmup):
+        one_step(False)
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    all_evs = []
+    w0 = time.perf_counter()
+    for _ in range(args.steps):
+        all_evs.append(one_step(True))
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - w0
+    clocks = sampler.stop() if sampler else None
+    if ws > 1:
+        torch.distributed.barrier()
+
+    total_ms = 0.0
+    total_bytes = 0
+    per_size = {}
+    dom_ms, dom_bytes, dom_n = 0.0, 0, 0
+    for evs in all_evs:
+        for (dims, perm, f, acc, e0, e1) in evs:
+            ms = e0.elapsed_time(e1)
+            b = case_bytes(dims, acc)
+            total_ms += ms
+            total_bytes += b
+            key = "x".join(map(str, dims))
+            a = per_size.setdefault(key, [0.0, 0])
+            a[0] += ms
+            a[1] += b
+            plan = S.plan(dims, perm)
+            if dims == (100, 100, 100, 100) and plan["kind"] == "tiled":
+                dom_ms += ms
+                dom_bytes += b
+                dom_n += 1
+    launches = len(cases) * args.steps
+    t_rank = total_ms / 1e3
+    if ws > 1:
+        t = torch.tensor([t_rank], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(t[0])
+    else:
+        t_max = t_rank
+    value = total_bytes * ws / t_max / 1e9
+
+    # e2e: same sweep through the C ABI with pinned host buffers
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        e2e = run_e2e(args, cases, torch, L, int_array, ctypes)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(args.cpu_seconds)
+
+    peak, peak_kind = peaks()
+    roof = None
+    if dom_n:
+        achieved = (dom_bytes / dom_n) / ((dom_ms / dom_n) / 1e3) / 1e9
+        tr = traffic_from_profile()
+        roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": tr,
+                "kernel": "spg_tiled (100^4, 18 tiled perms, sort+sortacc)",
+                "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, burst copy)"}
+    breakdown = {k: round(v[1] / (v[0] / 1e3) / 1e9, 1) for k, v in per_size.items()}
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(t_max * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded uniform(-1,1) FP64 in HBM)",
+        "config": {"workload": WORKLOAD, "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "flushed (512 MB write) before every launch whose tensors are < 2x L2; "
+                         "100^4 tensors exceed L2"},
+        "gpu_launches": launches,
+        "breakdown_gbs_by_size": breakdown,
+        "frac_of_hbm_peak": round(value / ws / peak, 4),
+        "roofline": roof,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "clocks": clocks,
+        "wall_s_timed_region": round(wall, 3),
+    }
+    return line
+
+
+def run_e2e(args, cases, torch, L, int_array, ctypes):
+    host = {}
+    for (dims, _, _, _) in cases:
+        if dims in host:
+            continue
+        n = 1
+        for d in dims:
+            n *= d
+        u = (torch.rand(n, dtype=torch.float64) * 2 - 1).pin_memory()
+        s = (torch.rand(n, dtype=torch.float64) * 2 - 1).pin_memory()
+        host[dims] = (u, s, n)
+    fac = ctypes.c_double()
+    h2d = d2h = 0
+    total_b = 0
+
+    def call(dims, perm, f, acc):
+        u, s, n = host[dims]
+        fac.value = f
+        ints = [ctypes.byref(ctypes.c_int(v)) for v in list(dims) + list(perm)]
+        fn = L.tce_sortacc_4_status if acc else L.tce_sort_4_status
+        rc = fn(ctypes.c_void_p(u.data_ptr()), ctypes.c_void_p(s.data_ptr()), *ints, ctypes.byref(fac))
+        if rc:
+            raise RuntimeError("tce_sort_4 failed %d" % rc)
+
+    for (dims, perm, f, acc) in cases[:48]:
+        call(dims, perm, f, acc)
+    steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        for (dims, perm, f, acc) in cases:
+            call(dims, perm, f, acc)
+            n = host[dims][2]
+            h2d += n * 8 * (2 if acc else 1)
+            d2h += n * 8
+            total_b += case_bytes(dims, acc)
+    dt = time.perf_counter() - t0
+    return {"value": round(total_b / dt / 1e9, 2), "unit": UNIT,
+            "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h // steps,
+            "steps": steps, "how": "tce_sort_4/tce_sortacc_4 C-ABI calls on pinned host "
+                                  "buffers, wall clock per sweep"}
+
+
+# ---------------------------------------------------------------------------
+def cpu_sweep_sample(budget_s: float, threads: int | None = None):
+    """The reference's C loop nests on the host cores: tune the loop order at
+    30^4 (all 24 per permutation, the reference's brute-force method), then
+    time a bounded sample of the sweep.  Returns (GB/s, cores, description)."""
+    import numpy as np
+    from oracle import refnests as R
+    from spaghetty_gb300.workloads import PERMS4, SORT4_DIMS
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    if R.load() is None:
+        return None
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    tdims = (30, 30, 30, 30)
+    n = 30 ** 4
+    rng = np.random.default_rng(3)
+    u = rng.uniform(-1, 1, n)
+    s = np.zeros(n)
+    best = {}
+    for perm in PERMS4:
+        bt, bl = 1e9, None
+        for lo in R.loops_for(4, perm):
+            R.call(perm, lo, u, s, tdims, 0.5, 0.0)
+            t0 = time.perf_counter()
+            R.call(perm, lo, u, s, tdims, 0.5, 0.0)
+            dt = time.perf_counter() - t0
+            if dt < bt:
+                bt, bl = dt, lo
+        best[perm] = bl
+    bufs = {}
+    for dims in SORT4_DIMS:
+        m = int(np.prod(dims))
+        bufs[dims] = (rng.uniform(-1, 1, m), rng.uniform(-1, 1, m))
+    total_b, total_t, calls = 0, 0.0, 0
+    order = [(d, p, acc) for d in SORT4_DIMS for p in PERMS4 for acc in (False, True)]
+    t_start = time.perf_counter()
+    for (dims, perm, acc) in order:
+        if time.perf_counter() - t_start > budget_s:
+            break
+        uu, ss = bufs[dims]
+        t0 = time.perf_counter()
+        R.call(perm, best[perm], uu, ss, dims, 0.5, 1.0 if acc else 0.0)
+        total_t += time.perf_counter() - t0
+        total_b += case_bytes(dims, acc)
+        calls += 1
+    desc = ("reference generated C nests (trunk/generator2.py emitter, OpenMP, gcc -O3 "
+            "-ffp-contract=off), best of 24 loop orders per perm tuned at 30^4; %d calls of the "
+            "sweep (sizes in order 20^4..100^4, 17x29x64x100; f=0.5; sort+sortacc) within %.0f s"
+            % (calls, budget_s))
+    return total_b / total_t / 1e9, cores, desc
+
+
+def cpu_baseline(budget_s):
+    try:
+        r = cpu_sweep_sample(budget_s)
+    except Exception as e:  # noqa: BLE001
+        return {"value": None, "unit": UNIT, "error": str(e)[:200]}
+    if r is None:
+        return {"value": None, "unit": UNIT, "error": "reference nests unavailable"}
+    v, cores, desc = r
+    return {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": "reference",
+            "sample": desc}
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return None
+    from oracle import refnests as R
+    if R.load() is None:
+        return {"impl": "reference", "unavailable": "reference C nests could not be built here"}
+    per_step = max(2.0, min(12.0, 150.0 / max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        cpu_sweep_sample(per_step)
+    vals = []
+    t0 = time.perf_counter()
+    cores, desc = None, None
+    for _ in range(args.steps):
+        v, cores, desc = cpu_sweep_sample(per_step)
+        vals.append(v)
+    wall = time.perf_counter() - t0
+    value = statistics.median(vals)
+    return {
+        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": UNIT,
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(wall * 1e3 / args.steps, 1), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded uniform(-1,1) FP64)",
+        "config": {"workload": WORKLOAD, "parallelism": "host cores (OpenMP)"},
+        "cpu_baseline": {"value": round(value, 2), "unit": UNIT, "cores": cores,
+                         "kind": "reference", "sample": desc},
+        "e2e": {"value": round(value, 2), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        line = run_reference(args, ws, rank)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    if args.warmup < 3:
+        args.warmup = 3
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+    line = run_ours(args, ws, rank, local)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,226 @@
+/*
+ * spaghetty_gb300.h -- C ABI of the GB300 tensor-permutation library.
+ *
+ * Drop-in replacements for NWChem TCE's tensor sorts.  The input
+ * `unsorted` with dims (d1..dr) is a flat FP64 buffer whose LAST index is
+ * stride-1 (equivalently the Fortran array u(dr,...,d1)); for the 1-based
+ * permutation (p1..pr) the output `sorted` has dims (d_{p1}..d_{pr}) and
+ *     sort:    sorted[j_{p1},...,j_{pr}] = unsorted[j1,...,jr] * factor
+ *     sortacc: sorted[j_{p1},...,j_{pr}] = sorted[...] + unsorted[j1,...,jr] * factor
+ * with the product rounded once and the sum rounded once (no FMA), so results
+ * are bit-identical to the reference's FP64 loop nests.
+ *
+ * Pointers may be device pointers (the kernel runs in place on the GPU) or
+ * host pointers (staged through cached device buffers).  The Fortran-style
+ * void entry points are synchronous: when they return, `sorted` holds the
+ * result.  They never abort; an error is printed once per call to stderr,
+ * `sorted` is left untouched where possible, and the code is kept for
+ * spaghetty_last_error().  Dims and permutation are 4-byte integers passed
+ * by reference, as the reference's default-integer Fortran callers do.
+ */
+#ifndef SPAGHETTY_GB300_H
+#define SPAGHETTY_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define SPAGHETTY_OK                0
+#define SPAGHETTY_ERR_RANK          1  /* rank outside 1..8                       */
+#define SPAGHETTY_ERR_PERM          2  /* permutation not a bijection of 1..r     */
+#define SPAGHETTY_ERR_DIMS          3  /* a dimension <= 0                        */
+#define SPAGHETTY_ERR_OVERFLOW      4  /* element count overflows int64           */
+#define SPAGHETTY_ERR_NULL          5  /* null pointer with a non-empty tensor    */
+#define SPAGHETTY_ERR_ALIAS         6  /* unsorted and sorted overlap             */
+#define SPAGHETTY_ERR_CUDA          7  /* a CUDA runtime call failed              */
+#define SPAGHETTY_ERR_MEMSPACE      8  /* pointer kinds not supported together    */
+#define SPAGHETTY_ERR_CONFIG        9  /* invalid kernel configuration override   */
+#define SPAGHETTY_ERR_BATCH        10  /* invalid batch entry                     */
+#define SPAGHETTY_ERR_DEVICE       11  /* device-side status word reported error  */
+#define SPAGHETTY_ERR_NOKERNEL     12  /* no compiled kernel variant fits         */
+
+/* ---- NWChem drop-ins (trunk/tce_sort4_switch.F:1-8; the Hirata routines in
+ *      branches/spaghetty3/python/tce_sort_hirata.F:62-63,143-144 and
+ *      branches/spaghetty2/tce_sortacc_hirata.F:49,120).  Names without and
+ *      with the trailing underscore, as GNU (-fno-underscoring) and
+ *      underscoring Fortran compilers emit (trunk/generator2.py:768,
+ *      trunk/tester_cutil.c:60-76). ---------------------------------------- */
+void tce_sort_4(const double *unsorted, double *sorted,
+                const int *a, const int *b, const int *c, const int *d,
+                const int *i, const int *j, const int *k, const int *l,
+                const double *factor);
+void tce_sort_4_(const double *unsorted, double *sorted,
+                 const int *a, const int *b, const int *c, const int *d,
+                 const int *i, const int *j, const int *k, const int *l,
+                 const double *factor);
+void tce_sortacc_4(const double *unsorted, double *sorted,
+                   const int *a, const int *b, const int *c, const int *d,
+                   const int *i, const int *j, const int *k, const int *l,
+                   const double *factor);
+void tce_sortacc_4_(const double *unsorted, double *sorted,
+                    const int *a, const int *b, const int *c, const int *d,
+                    const int *i, const int *j, const int *k, const int *l,
+                    const double *factor);
+void tce_sort_6(const double *unsorted, double *sorted,
+                const int *a, const int *b, const int *c, const int *d,
+                const int *e, const int *f,
+                const int *i, const int *j, const int *k, const int *l,
+                const int *m, const int *n, const double *factor);
+void tce_sort_6_(const double *unsorted, double *sorted,
+                 const int *a, const int *b, const int *c, const int *d,
+                 const int *e, const int *f,
+                 const int *i, const int *j, const int *k, const int *l,
+                 const int *m, const int *n, const double *factor);
+void tce_sortacc_6(const double *unsorted, double *sorted,
+                   const int *a, const int *b, const int *c, const int *d,
+                   const int *e, const int *f,
+                   const int *i, const int *j, const int *k, const int *l,
+                   const int *m, const int *n, const double *factor);
+void tce_sortacc_6_(const double *unsorted, double *sorted,
+                    const int *a, const int *b, const int *c, const int *d,
+                    const int *e, const int *f,
+                    const int *i, const int *j, const int *k, const int *l,
+                    const int *m, const int *n, const double *factor);
+
+/* Rank 2 and rank 8 members of the family (trunk/old_sort.f:10-31,236-478,
+ * 489-510,715-957; tce_sort_hirata.F:22-61,303). */
+void tce_sort_2(const double *unsorted, double *sorted, const int *a, const int *b,
+                const int *i, const int *j, const double *factor);
+void tce_sort_2_(const double *unsorted, double *sorted, const int *a, const int *b,
+                 const int *i, const int *j, const double *factor);
+void tce_sortacc_2(const double *unsorted, double *sorted, const int *a, const int *b,
+                   const int *i, const int *j, const double *factor);
+void tce_sortacc_2_(const double *unsorted, double *sorted, const int *a, const int *b,
+                    const int *i, const int *j, const double *factor);
+void tce_sort_8(const double *unsorted, double *sorted,
+                const int *a, const int *b, const int *c, const int *d,
+                const int *e, const int *f, const int *g, const int *h,
+                const int *i, const int *j, const int *k, const int *l,
+                const int *m, const int *n, const int *o, const int *p,
+                const double *factor);
+void tce_sort_8_(const double *unsorted, double *sorted,
+                 const int *a, const int *b, const int *c, const int *d,
+                 const int *e, const int *f, const int *g, const int *h,
+                 const int *i, const int *j, const int *k, const int *l,
+                 const int *m, const int *n, const int *o, const int *p,
+                 const double *factor);
+void tce_sortacc_8(const double *unsorted, double *sorted,
+                   const int *a, const int *b, const int *c, const int *d,
+                   const int *e, const int *f, const int *g, const int *h,
+                   const int *i, const int *j, const int *k, const int *l,
+                   const int *m, const int *n, const int *o, const int *p,
+                   const double *factor);
+void tce_sortacc_8_(const double *unsorted, double *sorted,
+                    const int *a, const int *b, const int *c, const int *d,
+                    const int *e, const int *f, const int *g, const int *h,
+                    const int *i, const int *j, const int *k, const int *l,
+                    const int *m, const int *n, const int *o, const int *p,
+                    const double *factor);
+
+/* Status-returning forms of the rank-4/6 drop-ins: same arguments, return a
+ * SPAGHETTY_* code instead of printing (the reference's tce_sort4_switch.F
+ * :58-60 can only print 'something is wrong...' and return). */
+int tce_sort_4_status(const double *unsorted, double *sorted,
+                      const int *a, const int *b, const int *c, const int *d,
+                      const int *i, const int *j, const int *k, const int *l,
+                      const double *factor);
+int tce_sortacc_4_status(const double *unsorted, double *sorted,
+                         const int *a, const int *b, const int *c, const int *d,
+                         const int *i, const int *j, const int *k, const int *l,
+                         const double *factor);
+int tce_sort_6_status(const double *unsorted, double *sorted,
+                      const int *a, const int *b, const int *c, const int *d,
+                      const int *e, const int *f,
+                      const int *i, const int *j, const int *k, const int *l,
+                      const int *m, const int *n, const double *factor);
+int tce_sortacc_6_status(const double *unsorted, double *sorted,
+                         const int *a, const int *b, const int *c, const int *d,
+                         const int *e, const int *f,
+                         const int *i, const int *j, const int *k, const int *l,
+                         const int *m, const int *n, const double *factor);
+
+/* ---- generic entry points --------------------------------------------- */
+
+/* The generated nests' two-factor form trans_<perm>_loop_<order>(unsorted,
+ * sorted, dims..., factor, acc_factor) (trunk/generator2.py:57-130,
+ * trunk/generator6.py:79-134) for any rank 1..8:
+ *     acc_factor == 0:  sorted = factor*unsorted
+ *     acc_factor == 1:  sorted = sorted + factor*unsorted
+ *     otherwise:        sorted = acc_factor*sorted + factor*unsorted
+ * `dims` and `perm` are host arrays of `rank` ints (perm 1-based).
+ * Both tensor pointers must be device pointers; the work is enqueued on
+ * `stream` (a cudaStream_t, NULL = legacy default stream) and the call
+ * returns without waiting.  Returns a SPAGHETTY_* code. */
+int spaghetty_sort_async(int rank, const double *unsorted, double *sorted,
+                         const int *dims, const int *perm,
+                         double factor, double acc_factor, void *stream);
+
+/* Same, synchronous, accepting host or device pointers. */
+int spaghetty_sort(int rank, const double *unsorted, double *sorted,
+                   const int *dims, const int *perm,
+                   double factor, double acc_factor);
+
+/* Last error recorded by any call on this host thread (0 = none), and a
+ * static description of a code. */
+int spaghetty_last_error(void);
+const char *spaghetty_error_string(int code);
+
+/* ---- plans (host only, no GPU needed) --------------------------------- */
+
+typedef struct spaghetty_plan_info {
+    int kind;           /* 0 = empty, 1 = flat (rank <= 1 after folding),
+                           2 = direct (fastest index unchanged),
+                           3 = tiled transpose through shared memory */
+    int rank;           /* rank after dropping unit dims and fusing indices */
+    int64_t dims[8];    /* folded dims, input order, last is stride-1     */
+    int perm[8];        /* folded permutation, 0-based, output position -> input dim */
+    int box[8];         /* tile box length per folded dim                 */
+    int threads;        /* CTA size                                       */
+    int ept;            /* elements per thread per tile                   */
+    int64_t ntiles;     /* number of boxes covering the tensor            */
+    int run_in;         /* contiguous input elements per box row          */
+    int run_out;        /* contiguous output elements per box row         */
+    int pad_period;     /* shared-memory padding: one word every N (0=none) */
+    int masked;         /* 1 when boundary boxes need element masks      */
+    int grid;           /* CTAs launched                                  */
+    int vec;            /* 2 when 16-byte vector accesses are used        */
+} spaghetty_plan_info;
+
+/* Fold and plan without launching.  op: 0 = sort, 1 = sortacc, 2 = general
+ * acc_factor.  Returns a SPAGHETTY_* code. */
+int spaghetty_plan_query(int rank, const int *dims, const int *perm, int op,
+                         spaghetty_plan_info *out);
+
+/* Host-side index-safety check of a plan, needing no GPU: replays the exact
+ * launch parameters through the kernels' own index functions, moving element
+ * indices instead of values, and returns SPAGHETTY_OK only if every global
+ * read and write lies inside the tensors, every shared-memory index inside
+ * the staging tile, and every output element is written exactly once from
+ * the input element the permutation maps to it.  stats (may be NULL)
+ * receives {reads, writes, boxes, staging elements}.  Tensors up to 2^27
+ * elements.  Returns SPAGHETTY_ERR_CONFIG on any violation. */
+int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, int num_sms,
+                          int64_t *stats);
+
+/* Autotuner hook: force the tile box / block shape for subsequent calls
+ * with the same folded (dims, perm, op).  box[] is indexed by folded dim;
+ * threads in {128,256,512}; ept in {1,2,4,8}.  Pass box == NULL to clear
+ * every override.  Returns a SPAGHETTY_* code. */
+int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op,
+                       const int *box, int threads, int ept);
+
+/* Host-side self checks of the planner's integer helpers (fast division by
+ * invariant divisors).  Returns 0 when they pass.  Needs no GPU. */
+int spaghetty_selftest(void);
+
+/* Library version string. */
+const char *spaghetty_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPAGHETTY_GB300_H */

@@ -1,0 +1,550 @@
+// api.cu -- the C ABI: NWChem drop-ins, generic entry points, dispatch.
+//
+// The reference's boundary is trunk/tce_sort4_switch.F:1-62 (tce_sort_4 maps
+// the permutation to the tuned loop nest; an unknown permutation prints
+// 'something is wrong...' and returns).  Here every entry point validates,
+// folds and plans on the host (plan.cpp), then launches one of the compiled
+// kernel variants (kernels.cuh, instantiated by generator.py).
+#include "../../include/spaghetty_gb300.h"
+#include "kernels.cuh"
+#include "plan.h"
+
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+const SpgKernelEntry *spg_kernels_op0(int *n);
+const SpgKernelEntry *spg_kernels_op1(int *n);
+const SpgKernelEntry *spg_kernels_op2(int *n);
+const SpgKernelEntry *spg_kernels_op3(int *n);
+const SpgKernelEntry *spg_kernels_op4(int *n);
+
+namespace {
+
+thread_local int g_last_error = 0;
+
+int record(int rc) {
+    g_last_error = rc;
+    return rc;
+}
+
+std::mutex g_mu;
+
+struct TuneOverride {
+    int box[SPG_MAXR];
+    int threads, ept;
+};
+std::map<std::string, TuneOverride> g_tune;
+std::map<int, int> g_sms;
+std::map<std::pair<const void *, int>, int> g_occ;
+
+const SpgKernelEntry *find_kernel(int kind, int op, int nt, int ept) {
+    static const SpgKernelEntry *tabs[OP_COUNT];
+    static int counts[OP_COUNT];
+    static std::once_flag once;
+    std::call_once(once, [] {
+        tabs[0] = spg_kernels_op0(&counts[0]);
+        tabs[1] = spg_kernels_op1(&counts[1]);
+        tabs[2] = spg_kernels_op2(&counts[2]);
+        tabs[3] = spg_kernels_op3(&counts[3]);
+        tabs[4] = spg_kernels_op4(&counts[4]);
+    });
+    if (op < 0 || op >= OP_COUNT) return nullptr;
+    for (int i = 0; i < counts[op]; ++i) {
+        const SpgKernelEntry &e = tabs[op][i];
+        if (e.kind == kind && e.threads == nt && e.ept == ept) return &e;
+    }
+    return nullptr;
+}
+
+int device_sms(int dev) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto it = g_sms.find(dev);
+    if (it != g_sms.end()) return it->second;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    g_sms[dev] = sms;
+    return sms;
+}
+
+int occupancy(const SpgKernelEntry *k, int smem) {
+    std::lock_guard<std::mutex> lk(g_mu);
+    auto key = std::make_pair(k->fn, smem);
+    auto it = g_occ.find(key);
+    if (it != g_occ.end()) return it->second;
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, k->threads, smem) != cudaSuccess) {
+        cudaGetLastError();
+        nb = 1;
+    }
+    if (nb < 1) nb = 1;
+    g_occ[key] = nb;
+    return nb;
+}
+
+std::string tune_key(const Folded &fo, int op) {
+    const int cls = (op == OP_COPY || op == OP_SCALE) ? 0 : (op == OP_GEN ? 2 : 1);
+    std::string k = std::to_string(fo.rank) + ":";
+    for (int d = 0; d < fo.rank; ++d) k += std::to_string(fo.D[d]) + ",";
+    k += ":";
+    for (int d = 0; d < fo.rank; ++d) k += std::to_string(fo.P[d]) + ",";
+    k += ":" + std::to_string(cls);
+    return k;
+}
+
+int make_plan(int rank, const int *dims, const int *perm, double f, double g, int sms, Plan *pl) {
+    Folded fo;
+    int rc = spg_fold(rank, dims, perm, &fo);
+    if (rc) return rc;
+    const int op = spg_choose_op(f, g);
+    TuneOverride ov;
+    bool have = false;
+    if (!fo.empty && fo.rank >= 2) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        auto it = g_tune.find(tune_key(fo, op));
+        if (it != g_tune.end()) { ov = it->second; have = true; }
+    }
+    rc = have ? spg_plan(fo, op, ov.box, ov.threads, ov.ept, sms, pl)
+              : spg_plan(fo, op, nullptr, 0, 0, sms, pl);
+    if (rc) return rc;
+    return spg_build_params(pl, f, g);
+}
+
+bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) {
+    if (pl.kind == KIND_EMPTY) return SPAGHETTY_OK;
+    const int sms = device_sms(dev);
+    cudaError_t err;
+    if (pl.kind == KIND_FLAT) {
+        const int vec = (aligned16(u) && aligned16(s)) ? 2 : 1;
+        const SpgKernelEntry *k = find_kernel(KIND_FLAT, pl.op, 256, vec);
+        if (!k) return SPAGHETTY_ERR_NOKERNEL;
+        int64_t n = pl.fo.nelem;
+        int64_t work = (n / vec + 255) / 256;
+        int grid = (int)std::min<int64_t>(std::max<int64_t>(work, 1), (int64_t)sms * 8);
+        double f = pl.kp.f, g = pl.kp.g;
+        void *args[] = {(void *)&u, (void *)&s, (void *)&n, (void *)&f, (void *)&g};
+        pl.grid = grid;
+        err = cudaLaunchKernel(k->fn, dim3(grid), dim3(256), args, 0, st);
+    } else {
+        const SpgKernelEntry *k = find_kernel(pl.kind, pl.op, pl.threads, pl.ept);
+        if (!k) return SPAGHETTY_ERR_NOKERNEL;
+        if (pl.smem_bytes > 48 * 1024) {
+            if (cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     pl.smem_bytes) != cudaSuccess) {
+                cudaGetLastError();
+                return SPAGHETTY_ERR_CUDA;
+            }
+        }
+        const int occ = occupancy(k, pl.smem_bytes);
+        int64_t grid = std::min<int64_t>((int64_t)pl.kp.ntiles, (int64_t)sms * occ);
+        if (grid < 1) grid = 1;
+        pl.grid = (int)grid;
+        void *args[] = {(void *)&u, (void *)&s, (void *)&pl.kp};
+        err = cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(pl.threads), args,
+                               (size_t)pl.smem_bytes, st);
+    }
+    if (err != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    return SPAGHETTY_OK;
+}
+
+bool overlaps(const double *a, const double *b, int64_t n) {
+    const uintptr_t a0 = (uintptr_t)a, a1 = a0 + (uintptr_t)n * sizeof(double);
+    const uintptr_t b0 = (uintptr_t)b, b1 = b0 + (uintptr_t)n * sizeof(double);
+    return a0 < b1 && b0 < a1;
+}
+
+// Where a pointer lives.  0 = host memory (pageable or pinned), 1 = memory a
+// kernel on `dev` may access (device or managed).
+int classify(const void *p, int *dev) {
+    cudaPointerAttributes at;
+    std::memset(&at, 0, sizeof(at));
+    cudaError_t e = cudaPointerGetAttributes(&at, p);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+        *dev = at.device;
+        return 1;
+    }
+    return 0;
+}
+
+// Cached staging buffers for host-pointer calls, per device (grow-only).
+struct Staging {
+    double *u = nullptr, *s = nullptr;
+    size_t nu = 0, ns = 0;
+};
+std::map<int, Staging> g_stage;
+std::mutex g_stage_mu;
+
+int grow(double **p, size_t *cap, size_t n) {
+    if (*cap >= n) return SPAGHETTY_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    if (cudaMalloc((void **)p, n * sizeof(double)) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return SPAGHETTY_ERR_CUDA;
+    }
+    *cap = n;
+    return SPAGHETTY_OK;
+}
+
+struct DeviceGuard {
+    int old = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&old) != cudaSuccess) { cudaGetLastError(); old = -1; }
+        if (dev >= 0 && dev != old) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (old >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != old) cudaSetDevice(old);
+    }
+};
+
+int sort_sync(int rank, const double *u, double *s, const int *dims, const int *perm,
+              double f, double g) {
+    Folded fo;
+    int rc = spg_fold(rank, dims, perm, &fo);
+    if (rc) return rc;
+    if (fo.empty) return SPAGHETTY_OK;
+    if (!u || !s) return SPAGHETTY_ERR_NULL;
+    if (overlaps(u, s, fo.nelem)) return SPAGHETTY_ERR_ALIAS;
+    int du = -1, ds = -1;
+    const int ku = classify(u, &du), ks = classify(s, &ds);
+    if (ku < 0 || ks < 0) return SPAGHETTY_ERR_CUDA;
+    int dev = ku == 1 ? du : (ks == 1 ? ds : -1);
+    if (ku == 1 && ks == 1 && du != ds) return SPAGHETTY_ERR_MEMSPACE;
+    DeviceGuard guard(dev);
+    if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
+    Plan pl;
+    rc = make_plan(rank, dims, perm, f, g, device_sms(dev), &pl);
+    if (rc) return rc;
+    cudaStream_t st = 0;  // legacy default stream: ordered after prior blocking-stream work
+    const size_t n = (size_t)fo.nelem;
+    const size_t bytes = n * sizeof(double);
+    if (ku == 1 && ks == 1) {
+        rc = launch_plan(pl, u, s, st, dev);
+        if (rc) return rc;
+        if (cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
+        return SPAGHETTY_OK;
+    }
+    std::lock_guard<std::mutex> lk(g_stage_mu);
+    Staging &sg = g_stage[dev];
+    const double *du_ptr = u;
+    double *ds_ptr = s;
+    if (ku == 0) {
+        if ((rc = grow(&sg.u, &sg.nu, n))) return rc;
+        if (cudaMemcpyAsync(sg.u, u, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) goto cuda_fail;
+        du_ptr = sg.u;
+    }
+    if (ks == 0) {
+        if ((rc = grow(&sg.s, &sg.ns, n))) return rc;
+        if (pl.op != OP_COPY && pl.op != OP_SCALE)
+            if (cudaMemcpyAsync(sg.s, s, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) goto cuda_fail;
+        ds_ptr = sg.s;
+    }
+    rc = launch_plan(pl, du_ptr, ds_ptr, st, dev);
+    if (rc) {
+        cudaStreamSynchronize(st);
+        return rc;
+    }
+    if (ks == 0)
+        if (cudaMemcpyAsync(s, sg.s, bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) goto cuda_fail;
+    if (cudaStreamSynchronize(st) != cudaSuccess) goto cuda_fail;
+    return SPAGHETTY_OK;
+cuda_fail:
+    cudaGetLastError();
+    cudaStreamSynchronize(st);
+    cudaGetLastError();
+    return SPAGHETTY_ERR_CUDA;
+}
+
+void report(const char *who, int rc, int rank, const int *perm) {
+    if (rc == SPAGHETTY_OK) return;
+    if (rc == SPAGHETTY_ERR_PERM) {
+        // the reference's only diagnostic (trunk/tce_sort4_switch.F:58-60)
+        std::fprintf(stderr, " something is wrong...\n");
+    }
+    std::fprintf(stderr, "spaghetty_gb300: %s: %s (permutation", who, spaghetty_error_string(rc));
+    for (int q = 0; q < rank; ++q) std::fprintf(stderr, " %d", perm[q]);
+    std::fprintf(stderr, ")\n");
+}
+
+int call_r(const char *who, bool print, int rank, const double *u, double *s, const int *dims,
+           const int *perm, double f, double g) {
+    int rc = sort_sync(rank, u, s, dims, perm, f, g);
+    record(rc);
+    if (print) report(who, rc, rank, perm);
+    return rc;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char *spaghetty_error_string(int code) {
+    switch (code) {
+        case SPAGHETTY_OK: return "ok";
+        case SPAGHETTY_ERR_RANK: return "rank outside 1..8";
+        case SPAGHETTY_ERR_PERM: return "permutation is not a bijection of 1..rank";
+        case SPAGHETTY_ERR_DIMS: return "negative dimension";
+        case SPAGHETTY_ERR_OVERFLOW: return "element count overflows int64";
+        case SPAGHETTY_ERR_NULL: return "null pointer";
+        case SPAGHETTY_ERR_ALIAS: return "unsorted and sorted overlap";
+        case SPAGHETTY_ERR_CUDA: return "CUDA runtime error";
+        case SPAGHETTY_ERR_MEMSPACE: return "pointers on different devices";
+        case SPAGHETTY_ERR_CONFIG: return "invalid kernel configuration";
+        case SPAGHETTY_ERR_BATCH: return "invalid batch entry";
+        case SPAGHETTY_ERR_DEVICE: return "device status word reported an error";
+        case SPAGHETTY_ERR_NOKERNEL: return "no compiled kernel variant fits";
+        default: return "unknown error";
+    }
+}
+
+int spaghetty_last_error(void) { return g_last_error; }
+
+const char *spaghetty_version(void) { return "spaghetty_gb300 0.1 (sm_103a)"; }
+
+int spaghetty_selftest(void) { return spg_selftest_host(); }
+
+int spaghetty_sort_async(int rank, const double *unsorted, double *sorted, const int *dims,
+                         const int *perm, double factor, double acc_factor, void *stream) {
+    Folded fo;
+    int rc = spg_fold(rank, dims, perm, &fo);
+    if (rc) return record(rc);
+    if (fo.empty) return record(SPAGHETTY_OK);
+    if (!unsorted || !sorted) return record(SPAGHETTY_ERR_NULL);
+    if (overlaps(unsorted, sorted, fo.nelem)) return record(SPAGHETTY_ERR_ALIAS);
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return record(SPAGHETTY_ERR_CUDA); }
+    Plan pl;
+    rc = make_plan(rank, dims, perm, factor, acc_factor, device_sms(dev), &pl);
+    if (rc) return record(rc);
+    return record(launch_plan(pl, unsorted, sorted, (cudaStream_t)stream, dev));
+}
+
+int spaghetty_sort(int rank, const double *unsorted, double *sorted, const int *dims,
+                   const int *perm, double factor, double acc_factor) {
+    return record(sort_sync(rank, unsorted, sorted, dims, perm, factor, acc_factor));
+}
+
+int spaghetty_plan_query(int rank, const int *dims, const int *perm, int op,
+                         spaghetty_plan_info *out) {
+    if (!out) return SPAGHETTY_ERR_NULL;
+    std::memset(out, 0, sizeof(*out));
+    const double f = 0.5, g = op == 0 ? 0.0 : (op == 1 ? 1.0 : 2.0);
+    Plan pl;
+    int rc = make_plan(rank, dims, perm, f, g, 152, &pl);
+    if (rc) return rc;
+    out->kind = pl.kind;
+    out->rank = pl.fo.rank;
+    for (int d = 0; d < pl.fo.rank; ++d) {
+        out->dims[d] = pl.fo.D[d];
+        out->perm[d] = pl.fo.P[d];
+        out->box[d] = pl.box[d];
+    }
+    out->threads = pl.threads;
+    out->ept = pl.ept;
+    out->ntiles = pl.kp.ntiles;
+    out->run_in = pl.run_in;
+    out->run_out = pl.run_out;
+    out->pad_period = pl.kp.pad;
+    out->masked = pl.masked;
+    out->grid = 0;
+    out->vec = 0;
+    return SPAGHETTY_OK;
+}
+
+int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, int num_sms,
+                          int64_t *stats) {
+    // Replays, on the host, the index arithmetic of the exact KParams a
+    // launch would receive (spg_box / spg_walk are the kernels' own
+    // functions), moving element INDICES instead of values.
+    const double f = 0.5, g = op == 0 ? 0.0 : (op == 1 ? 1.0 : 2.0);
+    Plan pl;
+    int rc = make_plan(rank, dims, perm, f, g, num_sms > 0 ? num_sms : 152, &pl);
+    if (rc) return rc;
+    if (stats) for (int q = 0; q < 4; ++q) stats[q] = 0;
+    if (pl.kind == KIND_EMPTY || pl.kind == KIND_FLAT) return SPAGHETTY_OK;
+    const KParams &kp = pl.kp;
+    const Folded &fo = pl.fo;
+    const int64_t n = fo.nelem;
+    if (n > ((int64_t)1 << 27)) return SPAGHETTY_ERR_CONFIG;
+    const int R = fo.rank;
+    int64_t istr[SPG_MAXR];
+    {
+        int64_t s = 1;
+        for (int d = R - 1; d >= 0; --d) { istr[d] = s; s *= fo.D[d]; }
+    }
+    std::vector<int64_t> got((size_t)n, -1);
+    const int64_t smem_elems = pl.smem_bytes / (int64_t)sizeof(double);
+    std::vector<int64_t> sm((size_t)std::max<int64_t>(smem_elems, 1), -2);
+    int64_t reads = 0, writes = 0;
+    for (uint32_t t = 0; t < kp.ntiles; ++t) {
+        int64_t ib, ob;
+        uint32_t limA, limB;
+        spg_box(kp, t, ib, ob, limA, limB);
+        for (uint32_t e = 0; e < (uint32_t)kp.vol; ++e) {
+            int32_t a, b, lin;
+            uint32_t pk;
+            spg_walk(kp.ld, e, a, b, lin, pk);
+            const bool v = spg_valid(pk, limA, limB);
+            if (pl.kind == KIND_DIRECT) {
+                if (!v) continue;
+                const int64_t src = ib + a, dst = ob + b;
+                if (src < 0 || src >= n || dst < 0 || dst >= n) return SPAGHETTY_ERR_CONFIG;
+                if (got[(size_t)dst] != -1) return SPAGHETTY_ERR_CONFIG;
+                got[(size_t)dst] = src;
+                ++reads; ++writes;
+            } else {
+                const int64_t w = (int64_t)e + (kp.pad ? (int64_t)e / kp.pad : 0);
+                if (w < 0 || w >= smem_elems) return SPAGHETTY_ERR_CONFIG;
+                if (v) {
+                    const int64_t src = ib + a;
+                    if (src < 0 || src >= n) return SPAGHETTY_ERR_CONFIG;
+                    sm[(size_t)w] = src;
+                    ++reads;
+                } else {
+                    sm[(size_t)w] = -3;
+                }
+            }
+        }
+        if (pl.kind == KIND_TILED) {
+            for (uint32_t e = 0; e < (uint32_t)kp.vol; ++e) {
+                int32_t a, b, lin;
+                uint32_t pk;
+                spg_walk(kp.st, e, a, b, lin, pk);
+                if (!spg_valid(pk, limA, limB)) continue;
+                const int64_t r = (int64_t)lin + (kp.pad ? (int64_t)lin / kp.pad : 0);
+                if (r < 0 || r >= smem_elems) return SPAGHETTY_ERR_CONFIG;
+                const int64_t dst = ob + a;
+                if (dst < 0 || dst >= n) return SPAGHETTY_ERR_CONFIG;
+                if (got[(size_t)dst] != -1 || sm[(size_t)r] < 0) return SPAGHETTY_ERR_CONFIG;
+                got[(size_t)dst] = sm[(size_t)r];
+                ++writes;
+            }
+        }
+    }
+    // every output element written once, from the input element the
+    // permutation maps to it
+    for (int64_t o = 0; o < n; ++o) {
+        int64_t rem = o, src = 0;
+        for (int q = R - 1; q >= 0; --q) {
+            const int64_t ext = fo.D[fo.P[q]];
+            src += (rem % ext) * istr[fo.P[q]];
+            rem /= ext;
+        }
+        if (got[(size_t)o] != src) return SPAGHETTY_ERR_CONFIG;
+    }
+    if (stats) {
+        stats[0] = reads;
+        stats[1] = writes;
+        stats[2] = kp.ntiles;
+        stats[3] = smem_elems;
+    }
+    return SPAGHETTY_OK;
+}
+
+int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const int *box,
+                       int threads, int ept) {
+    if (!box) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_tune.clear();
+        return SPAGHETTY_OK;
+    }
+    Folded fo;
+    int rc = spg_fold(rank, dims, perm, &fo);
+    if (rc) return rc;
+    if (fo.empty || fo.rank < 2) return SPAGHETTY_ERR_CONFIG;
+    if (threads != 128 && threads != 256 && threads != 512) return SPAGHETTY_ERR_CONFIG;
+    if (ept != 1 && ept != 2 && ept != 4 && ept != 8) return SPAGHETTY_ERR_CONFIG;
+    const int opc = op == 0 ? OP_SCALE : (op == 1 ? OP_ACCF : OP_GEN);
+    Plan pl;
+    rc = spg_plan(fo, opc, box, threads, ept, 152, &pl);
+    if (rc) return rc;
+    rc = spg_build_params(&pl, 0.5, 1.0);
+    if (rc) return rc;
+    TuneOverride ov;
+    for (int d = 0; d < SPG_MAXR; ++d) ov.box[d] = d < fo.rank ? box[d] : 1;
+    ov.threads = threads;
+    ov.ept = ept;
+    std::lock_guard<std::mutex> lk(g_mu);
+    g_tune[tune_key(fo, opc)] = ov;
+    return SPAGHETTY_OK;
+}
+
+// ---- NWChem drop-ins ------------------------------------------------------
+#define SPG_R4_ARGS                                                                        \
+    const double *unsorted, double *sorted, const int *a, const int *b, const int *c,       \
+        const int *d, const int *i, const int *j, const int *k, const int *l,               \
+        const double *factor
+#define SPG_R6_ARGS                                                                        \
+    const double *unsorted, double *sorted, const int *a, const int *b, const int *c,       \
+        const int *d, const int *e, const int *f, const int *i, const int *j, const int *k, \
+        const int *l, const int *m, const int *n, const double *factor
+#define SPG_R8_ARGS                                                                        \
+    const double *unsorted, double *sorted, const int *a, const int *b, const int *c,       \
+        const int *d, const int *e, const int *f, const int *g, const int *h, const int *i, \
+        const int *j, const int *k, const int *l, const int *m, const int *n, const int *o, \
+        const int *p, const double *factor
+
+static int r2(const char *w, bool pr, const double *u, double *s, const int *a, const int *b,
+              const int *i, const int *j, const double *fac, double g) {
+    const int dm[2] = {*a, *b}, pm[2] = {*i, *j};
+    return call_r(w, pr, 2, u, s, dm, pm, *fac, g);
+}
+static int r4(const char *w, bool pr, SPG_R4_ARGS, double g) {
+    const int dm[4] = {*a, *b, *c, *d}, pm[4] = {*i, *j, *k, *l};
+    return call_r(w, pr, 4, unsorted, sorted, dm, pm, *factor, g);
+}
+static int r6(const char *w, bool pr, SPG_R6_ARGS, double g) {
+    const int dm[6] = {*a, *b, *c, *d, *e, *f}, pm[6] = {*i, *j, *k, *l, *m, *n};
+    return call_r(w, pr, 6, unsorted, sorted, dm, pm, *factor, g);
+}
+static int r8(const char *w, bool pr, SPG_R8_ARGS, double gg) {
+    const int dm[8] = {*a, *b, *c, *d, *e, *f, *g, *h}, pm[8] = {*i, *j, *k, *l, *m, *n, *o, *p};
+    return call_r(w, pr, 8, unsorted, sorted, dm, pm, *factor, gg);
+}
+
+void tce_sort_2(const double *u, double *s, const int *a, const int *b, const int *i, const int *j, const double *f) { r2("tce_sort_2", true, u, s, a, b, i, j, f, 0.0); }
+void tce_sort_2_(const double *u, double *s, const int *a, const int *b, const int *i, const int *j, const double *f) { r2("tce_sort_2", true, u, s, a, b, i, j, f, 0.0); }
+void tce_sortacc_2(const double *u, double *s, const int *a, const int *b, const int *i, const int *j, const double *f) { r2("tce_sortacc_2", true, u, s, a, b, i, j, f, 1.0); }
+void tce_sortacc_2_(const double *u, double *s, const int *a, const int *b, const int *i, const int *j, const double *f) { r2("tce_sortacc_2", true, u, s, a, b, i, j, f, 1.0); }
+
+void tce_sort_4(SPG_R4_ARGS) { r4("tce_sort_4", true, unsorted, sorted, a, b, c, d, i, j, k, l, factor, 0.0); }
+void tce_sort_4_(SPG_R4_ARGS) { r4("tce_sort_4", true, unsorted, sorted, a, b, c, d, i, j, k, l, factor, 0.0); }
+void tce_sortacc_4(SPG_R4_ARGS) { r4("tce_sortacc_4", true, unsorted, sorted, a, b, c, d, i, j, k, l, factor, 1.0); }
+void tce_sortacc_4_(SPG_R4_ARGS) { r4("tce_sortacc_4", true, unsorted, sorted, a, b, c, d, i, j, k, l, factor, 1.0); }
+int tce_sort_4_status(SPG_R4_ARGS) { return r4("tce_sort_4", false, unsorted, sorted, a, b, c, d, i, j, k, l, factor, 0.0); }
+int tce_sortacc_4_status(SPG_R4_ARGS) { return r4("tce_sortacc_4", false, unsorted, sorted, a, b, c, d, i, j, k, l, factor, 1.0); }
+
+void tce_sort_6(SPG_R6_ARGS) { r6("tce_sort_6", true, unsorted, sorted, a, b, c, d, e, f, i, j, k, l, m, n, factor, 0.0); }
+void tce_sort_6_(SPG_R6_ARGS) { r6("tce_sort_6", true, unsorted, sorted, a, b, c, d, e, f, i, j, k, l, m, n, factor, 0.0); }
+void tce_sortacc_6(SPG_R6_ARGS) { r6("tce_sortacc_6", true, unsorted, sorted, a, b, c, d, e, f, i, j, k, l, m, n, factor, 1.0); }
+void tce_sortacc_6_(SPG_R6_ARGS) { r6("tce_sortacc_6", true, unsorted, sorted, a, b, c, d, e, f, i, j, k, l, m, n, factor, 1.0); }
+int tce_sort_6_status(SPG_R6_ARGS) { return r6("tce_sort_6", false, unsorted, sorted, a, b, c, d, e, f, i, j, k, l, m, n, factor, 0.0); }
+int tce_sortacc_6_status(SPG_R6_ARGS) { return r6("tce_sortacc_6", false, unsorted, sorted, a, b, c, d, e, f, i, j, k, l, m, n, factor, 1.0); }
+
+void tce_sort_8(SPG_R8_ARGS) { r8("tce_sort_8", true, unsorted, sorted, a, b, c, d, e, f, g, h, i, j, k, l, m, n, o, p, factor, 0.0); }
+void tce_sort_8_(SPG_R8_ARGS) { r8("tce_sort_8", true, unsorted, sorted, a, b, c, d, e, f, g, h, i, j, k, l, m, n, o, p, factor, 0.0); }
+void tce_sortacc_8(SPG_R8_ARGS) { r8("tce_sortacc_8", true, unsorted, sorted, a, b, c, d, e, f, g, h, i, j, k, l, m, n, o, p, factor, 1.0); }
+void tce_sortacc_8_(SPG_R8_ARGS) { r8("tce_sortacc_8", true, unsorted, sorted, a, b, c, d, e, f, g, h, i, j, k, l, m, n, o, p, factor, 1.0); }
+
+}  // extern "C"

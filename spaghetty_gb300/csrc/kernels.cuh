@@ -1,0 +1,262 @@
+// kernels.cuh -- sm_103a tensor-permutation kernels (FP64, bit-exact).
+//
+// Three kernel families cover every folded permutation:
+//   spg_flat    rank <= 1 after folding: identity permutation, a streaming
+//               copy/scale/axpy (the reference's f_memcpy path,
+//               trunk/tester_cutil.c:51-76, trunk/generator3.py:182-210).
+//   spg_direct  the stride-1 index is unchanged and its rows are long: every
+//               element is read and written by the same thread, no staging.
+//   spg_tiled   everything else: a persistent CTA walks the grid of boxes;
+//               per box it loads the elements in input order (coalesced
+//               runs), stages them in a padded shared-memory tile, and writes
+//               them in output order (coalesced runs).
+// Per-element box offsets are computed once per CTA (fast division) and kept
+// in registers for all the boxes the CTA processes.
+//
+// Arithmetic is the reference's: one rounded product, then one rounded sum
+// (trunk/old_sort.f:58,537: y(ib) = y(ib) + x(ia)*s); __dmul_rn/__dadd_rn
+// forbid contraction into an FMA.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "plan.h"
+
+template <int OP>
+__device__ __forceinline__ double spg_apply(double x, double y, double f, double g) {
+    if (OP == OP_COPY) return x;
+    if (OP == OP_SCALE) return __dmul_rn(x, f);
+    if (OP == OP_ACC1) return __dadd_rn(y, x);
+    if (OP == OP_ACCF) return __dadd_rn(y, __dmul_rn(x, f));
+    return __dadd_rn(__dmul_rn(g, y), __dmul_rn(f, x));   // OP_GEN
+}
+
+template <int OP>
+struct spg_reads_out { static constexpr bool value = (OP == OP_ACC1 || OP == OP_ACCF || OP == OP_GEN); };
+
+// Input is read exactly once: keep it out of L1 and mark it evict-first.
+__device__ __forceinline__ double spg_ld_in(const double *p) { return __ldcs(p); }
+__device__ __forceinline__ double spg_ld_out(const double *p) { return __ldcs(p); }
+__device__ __forceinline__ void spg_st_out(double *p, double v) { __stcs(p, v); }
+
+// Decompose a box-local element index along a walk.  Host-callable too, so
+// that spaghetty_plan_verify can replay the exact index arithmetic on the CPU.
+__host__ __device__ __forceinline__ void spg_walk(const BoxWalk &w, uint32_t e, int32_t &oa,
+                                         int32_t &ob, int32_t &lin, uint32_t &pk) {
+    oa = 0; ob = 0; lin = 0; pk = 0;
+#pragma unroll
+    for (int k = 0; k < SPG_MAXR; ++k) {
+        if (k < w.n) {
+            const uint32_t q = fd_div(e, w.len[k]);
+            const uint32_t c = e - q * w.len[k].d;
+            e = q;
+            oa += (int32_t)c * (int32_t)w.gs_a[k];
+            ob += (int32_t)c * (int32_t)w.gs_b[k];
+            lin += (int32_t)c * w.bs[k];
+            if (w.mpos[k] == 1) pk |= c << 16;
+            if (w.mpos[k] == 2) pk |= c;
+        }
+    }
+}
+
+// Box t -> base offsets and the element limits of the (at most two) dims
+// whose last box is partial.
+__host__ __device__ __forceinline__ void spg_box(const KParams &p, uint32_t t, int64_t &ib,
+                                        int64_t &ob, uint32_t &limA, uint32_t &limB) {
+    ib = 0; ob = 0;
+    limA = (uint32_t)p.lenA;
+    limB = (uint32_t)p.lenB;
+#pragma unroll
+    for (int k = 0; k < SPG_MAXR; ++k) {
+        if (k < p.grid.n) {
+            const uint32_t q = fd_div(t, p.grid.cnt[k]);
+            const uint32_t c = t - q * p.grid.cnt[k].d;
+            t = q;
+            ib += (int64_t)c * p.grid.in_step[k];
+            ob += (int64_t)c * p.grid.out_step[k];
+            if (p.grid.mpos[k] == 1) {
+                const int r = p.extA - (int)c * p.lenA;
+                limA = (uint32_t)(r < p.lenA ? r : p.lenA);
+            }
+            if (p.grid.mpos[k] == 2) {
+                const int r = p.extB - (int)c * p.lenB;
+                limB = (uint32_t)(r < p.lenB ? r : p.lenB);
+            }
+        }
+    }
+}
+
+__host__ __device__ __forceinline__ bool spg_valid(uint32_t pk, uint32_t limA, uint32_t limB) {
+    return (pk >> 16) < limA && (pk & 0xFFFFu) < limB;
+}
+
+#define SPG_INVALID 0xFFFFFFFFu
+
+// ---------------------------------------------------------------------------
+template <int NT, int EPT, int OP>
+__global__ void __launch_bounds__(NT)
+spg_tiled(const double *__restrict__ in, double *__restrict__ out,
+          const __grid_constant__ KParams p) {
+    extern __shared__ double sm[];
+    const uint32_t tid = threadIdx.x;
+    int32_t ioff[EPT], smw[EPT], ooff[EPT], smr[EPT];
+    uint32_t pkl[EPT], pks[EPT];
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+        const uint32_t e = tid + k * NT;
+        if (e < (uint32_t)p.vol) {
+            int32_t a, b, lin;
+            uint32_t pk;
+            spg_walk(p.ld, e, a, b, lin, pk);
+            ioff[k] = a;
+            smw[k] = (int32_t)e + (p.pad ? (int32_t)e / p.pad : 0);
+            pkl[k] = pk;
+            spg_walk(p.st, e, a, b, lin, pk);
+            ooff[k] = a;
+            smr[k] = lin + (p.pad ? lin / p.pad : 0);
+            pks[k] = pk;
+        } else {
+            ioff[k] = 0; smw[k] = 0; pkl[k] = SPG_INVALID;
+            ooff[k] = 0; smr[k] = 0; pks[k] = SPG_INVALID;
+        }
+    }
+    const double f = p.f, g = p.g;
+    for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        int64_t ib, ob;
+        uint32_t limA, limB;
+        spg_box(p, t, ib, ob, limA, limB);
+        const double *src = in + ib;
+        double *dst = out + ob;
+        double v[EPT];
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            v[k] = 0.0;
+            if (spg_valid(pkl[k], limA, limB)) v[k] = spg_ld_in(src + ioff[k]);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < EPT; ++k)
+            if (pkl[k] != SPG_INVALID) sm[smw[k]] = v[k];
+        __syncthreads();
+        double y[EPT];
+        if (spg_reads_out<OP>::value) {
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                y[k] = 0.0;
+                if (spg_valid(pks[k], limA, limB)) y[k] = spg_ld_out(dst + ooff[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            if (spg_valid(pks[k], limA, limB)) {
+                const double x = sm[smr[k]];
+                spg_st_out(dst + ooff[k], spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, f, g));
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+template <int NT, int EPT, int OP>
+__global__ void __launch_bounds__(NT)
+spg_direct(const double *__restrict__ in, double *__restrict__ out,
+           const __grid_constant__ KParams p) {
+    const uint32_t tid = threadIdx.x;
+    int32_t ioff[EPT], ooff[EPT];
+    uint32_t pkk[EPT];
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+        const uint32_t e = tid + k * NT;
+        if (e < (uint32_t)p.vol) {
+            int32_t a, b, lin;
+            uint32_t pk;
+            spg_walk(p.ld, e, a, b, lin, pk);
+            ioff[k] = a; ooff[k] = b; pkk[k] = pk;
+        } else {
+            ioff[k] = 0; ooff[k] = 0; pkk[k] = SPG_INVALID;
+        }
+    }
+    const double f = p.f, g = p.g;
+    for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        int64_t ib, ob;
+        uint32_t limA, limB;
+        spg_box(p, t, ib, ob, limA, limB);
+        const double *src = in + ib;
+        double *dst = out + ob;
+        double v[EPT], y[EPT];
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            v[k] = 0.0; y[k] = 0.0;
+            if (spg_valid(pkk[k], limA, limB)) {
+                v[k] = spg_ld_in(src + ioff[k]);
+                if (spg_reads_out<OP>::value) y[k] = spg_ld_out(dst + ooff[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < EPT; ++k)
+            if (spg_valid(pkk[k], limA, limB))
+                spg_st_out(dst + ooff[k], spg_apply<OP>(v[k], y[k], f, g));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Flat: n contiguous elements, identity order.  VEC = 2 uses 16-byte
+// accesses (both pointers 16-byte aligned); the odd tail element is handled
+// by thread 0 of block 0.
+template <int OP, int VEC>
+__global__ void __launch_bounds__(256)
+spg_flat(const double *__restrict__ in, double *__restrict__ out, int64_t n, double f,
+         double g) {
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (VEC == 2) {
+        const int64_t n2 = n >> 1;
+        const double2 *in2 = reinterpret_cast<const double2 *>(in);
+        double2 *out2 = reinterpret_cast<double2 *>(out);
+        int64_t j = i0;
+        for (; j + 3 * stride < n2; j += 4 * stride) {
+            double2 x[4], y[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                x[u] = __ldcs(in2 + j + u * stride);
+                if (spg_reads_out<OP>::value) y[u] = __ldcs(out2 + j + u * stride);
+                else y[u] = make_double2(0.0, 0.0);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                double2 r;
+                r.x = spg_apply<OP>(x[u].x, y[u].x, f, g);
+                r.y = spg_apply<OP>(x[u].y, y[u].y, f, g);
+                __stcs(out2 + j + u * stride, r);
+            }
+        }
+        for (; j < n2; j += stride) {
+            const double2 x = __ldcs(in2 + j);
+            double2 y = make_double2(0.0, 0.0);
+            if (spg_reads_out<OP>::value) y = __ldcs(out2 + j);
+            double2 r;
+            r.x = spg_apply<OP>(x.x, y.x, f, g);
+            r.y = spg_apply<OP>(x.y, y.y, f, g);
+            __stcs(out2 + j, r);
+        }
+        if ((n & 1) && i0 == 0) {
+            const double x = in[n - 1];
+            const double y = spg_reads_out<OP>::value ? out[n - 1] : 0.0;
+            out[n - 1] = spg_apply<OP>(x, y, f, g);
+        }
+    } else {
+        for (int64_t j = i0; j < n; j += stride) {
+            const double x = __ldcs(in + j);
+            const double y = spg_reads_out<OP>::value ? __ldcs(out + j) : 0.0;
+            __stcs(out + j, spg_apply<OP>(x, y, f, g));
+        }
+    }
+}
+
+// Table entry emitted by the generator for every compiled variant.
+struct SpgKernelEntry {
+    int kind;       // SpgKind
+    int op;         // SpgOp
+    int threads;
+    int ept;        // elements per thread (flat: vector width)
+    const void *fn;
+};

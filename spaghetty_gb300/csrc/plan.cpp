@@ -1,0 +1,428 @@
+// plan.cpp -- host-side folding and box planning (no CUDA calls).
+#include "plan.h"
+#include "../../include/spaghetty_gb300.h"
+
+#include <algorithm>
+#include <climits>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+static FastDiv make_fastdiv(uint32_t d) {
+    FastDiv f;
+    f.d = d ? d : 1;
+    uint32_t l = 0;
+    while (l < 32 && (1ull << l) < f.d) ++l;
+    f.l = l;
+    uint64_t num = ((uint64_t)1 << 32) * (((uint64_t)1 << l) - f.d);
+    f.m = (uint32_t)(num / f.d + 1);
+    return f;
+}
+
+// ---------------------------------------------------------------------------
+// Folding.  perm is 1-based (reference convention, trunk/old_sort.f:44-56).
+int spg_fold(int rank, const int *dims, const int *perm, Folded *out) {
+    std::memset(out, 0, sizeof(*out));
+    if (rank < 1 || rank > SPG_MAXR) return SPAGHETTY_ERR_RANK;
+    if (!dims || !perm) return SPAGHETTY_ERR_NULL;
+    bool seen[SPG_MAXR] = {false};
+    for (int q = 0; q < rank; ++q) {
+        int p = perm[q];
+        if (p < 1 || p > rank || seen[p - 1]) return SPAGHETTY_ERR_PERM;
+        seen[p - 1] = true;
+    }
+    int64_t n = 1;
+    bool empty = false;
+    for (int q = 0; q < rank; ++q) {
+        if (dims[q] < 0) return SPAGHETTY_ERR_DIMS;
+        if (dims[q] == 0) empty = true;
+    }
+    if (!empty) {
+        for (int q = 0; q < rank; ++q) {
+            if (n > INT64_MAX / dims[q]) return SPAGHETTY_ERR_OVERFLOW;
+            n *= dims[q];
+        }
+    }
+    out->nelem = empty ? 0 : n;
+    out->empty = empty;
+    if (empty) return SPAGHETTY_OK;
+
+    // 1. drop unit dims
+    int newidx[SPG_MAXR];
+    int64_t D1[SPG_MAXR];
+    int r1 = 0;
+    for (int d = 0; d < rank; ++d) {
+        if (dims[d] > 1) { newidx[d] = r1; D1[r1++] = dims[d]; }
+        else newidx[d] = -1;
+    }
+    int P1[SPG_MAXR];
+    int np = 0;
+    for (int q = 0; q < rank; ++q) {
+        int d = perm[q] - 1;
+        if (newidx[d] >= 0) P1[np++] = newidx[d];
+    }
+    // 2. fuse runs that are adjacent and ordered in both input and output
+    //    group g (output order) = consecutive output positions whose input
+    //    dims are consecutive increasing
+    int gstart[SPG_MAXR], glen[SPG_MAXR], ng = 0;
+    for (int q = 0; q < r1; ++q) {
+        if (q > 0 && P1[q] == P1[q - 1] + 1) { glen[ng - 1]++; }
+        else { gstart[ng] = q; glen[ng] = 1; ++ng; }
+    }
+    // groups sorted by their first input dim give the folded input order
+    int order[SPG_MAXR];
+    for (int g = 0; g < ng; ++g) order[g] = g;
+    std::sort(order, order + ng, [&](int a, int b) { return P1[gstart[a]] < P1[gstart[b]]; });
+    int pos_in[SPG_MAXR];
+    for (int k = 0; k < ng; ++k) pos_in[order[k]] = k;
+    out->rank = ng;
+    for (int k = 0; k < ng; ++k) {
+        int g = order[k];
+        int64_t e = 1;
+        for (int t = 0; t < glen[g]; ++t) e *= D1[P1[gstart[g]] + t];
+        out->D[k] = e;
+    }
+    for (int g = 0; g < ng; ++g) out->P[g] = pos_in[g];
+    return SPAGHETTY_OK;
+}
+
+int spg_choose_op(double f, double g) {
+    if (g == 0.0) return f == 1.0 ? OP_COPY : OP_SCALE;
+    if (g == 1.0) return f == 1.0 ? OP_ACC1 : OP_ACCF;
+    return OP_GEN;
+}
+
+// ---------------------------------------------------------------------------
+// Box selection.
+namespace {
+
+struct Shape {
+    int R;
+    int64_t D[SPG_MAXR];
+    int in_order[SPG_MAXR];   // input dims, fastest first
+    int out_order[SPG_MAXR];  // input dims in output order, fastest first
+};
+
+int64_t run_len(const Shape &s, const int64_t *L, const int *order) {
+    int64_t r = 1;
+    for (int q = 0; q < s.R; ++q) {
+        int d = order[q];
+        r *= L[d];
+        if (L[d] < s.D[d]) break;
+    }
+    return r;
+}
+
+int frontier(const Shape &s, const int64_t *L, const int *order) {
+    for (int q = 0; q < s.R; ++q)
+        if (L[order[q]] < s.D[order[q]]) return order[q];
+    return -1;
+}
+
+int64_t volume(const Shape &s, const int64_t *L) {
+    int64_t v = 1;
+    for (int d = 0; d < s.R; ++d) v *= L[d];
+    return v;
+}
+
+// smallest even split of D into boxes of length >= want
+int64_t split_len(int64_t D, int64_t want) {
+    if (want >= D) return D;
+    if (want < 1) want = 1;
+    int64_t nt = std::max<int64_t>(1, D / want);
+    return (D + nt - 1) / nt;
+}
+
+int64_t largest_divisor_le(int64_t D, int64_t v) {
+    for (int64_t x = std::min(D, v); x > 1; --x)
+        if (D % x == 0) return x;
+    return 1;
+}
+
+}  // namespace
+
+static const int kTRun = 32;      // minimum contiguous doubles per box row
+static const int kVMax = 4096;    // largest box (512 threads x 8)
+
+static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L) {
+    for (int d = 0; d < s.R; ++d) L[d] = 1;
+    // phase 1: both runs >= kTRun (or the whole extent of that side)
+    for (int it = 0; it < 64; ++it) {
+        int64_t vol = volume(s, L);
+        int64_t ri = run_len(s, L, s.in_order), ro = run_len(s, L, s.out_order);
+        int d = -1;
+        int64_t need = 0;
+        if (ri < kTRun && (d = frontier(s, L, s.in_order)) >= 0) {
+            need = (kTRun * L[d] + ri - 1) / ri;
+        } else if (ro < kTRun && (d = frontier(s, L, s.out_order)) >= 0) {
+            need = (kTRun * L[d] + ro - 1) / ro;
+        } else {
+            break;
+        }
+        int64_t nl = split_len(s.D[d], need);
+        if (vol / L[d] * nl > kVMax) nl = std::max<int64_t>(L[d], kVMax * L[d] / vol);
+        if (nl <= L[d]) break;
+        L[d] = nl;
+    }
+    // phase 2: grow the box towards a target volume that still leaves
+    // enough boxes to fill every SM a few times
+    int64_t target = nelem / (4 * (int64_t)std::max(1, num_sms));
+    target = std::max<int64_t>(256, std::min<int64_t>(2048, target));
+    for (int it = 0; it < 64; ++it) {
+        int64_t vol = volume(s, L);
+        if (vol >= target) break;
+        int64_t ri = run_len(s, L, s.in_order), ro = run_len(s, L, s.out_order);
+        int fi = frontier(s, L, s.in_order), fo = frontier(s, L, s.out_order);
+        int d = -1;
+        if (fi >= 0 && fo >= 0) d = (ro <= ri) ? fo : fi;
+        else if (fo >= 0) d = fo;
+        else if (fi >= 0) d = fi;
+        if (d < 0) break;
+        int64_t want = std::min<int64_t>(L[d] * 2, L[d] * std::max<int64_t>(2, target / vol));
+        int64_t nl = split_len(s.D[d], want);
+        if (vol / L[d] * nl > kVMax) nl = largest_divisor_le(s.D[d], kVMax * L[d] / vol);
+        if (nl <= L[d]) break;
+        L[d] = nl;
+    }
+    // at most two dims may end in a partial box (they carry element masks):
+    // keep the two frontier dims, round any other partial dim down to a divisor
+    const int fi = frontier(s, L, s.in_order), fo = frontier(s, L, s.out_order);
+    for (int d = 0; d < s.R; ++d)
+        if (L[d] < s.D[d] && s.D[d] % L[d] != 0 && d != fi && d != fo)
+            L[d] = largest_divisor_le(s.D[d], L[d]);
+}
+
+static int pick_block(int vol, int *threads, int *ept) {
+    static const int nts[3] = {256, 512, 128};
+    static const int epts[4] = {1, 2, 4, 8};
+    int best = INT_MAX, bt = 0, be = 0;
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 4; ++b) {
+            int cap = nts[a] * epts[b];
+            if (cap < vol) continue;
+            if (cap < best) { best = cap; bt = nts[a]; be = epts[b]; }
+        }
+    if (!bt) return SPAGHETTY_ERR_NOKERNEL;
+    *threads = bt;
+    *ept = be;
+    return SPAGHETTY_OK;
+}
+
+// Count shared-memory wavefronts of the store phase (8-byte words: a half
+// warp is served per wavefront when its 16 words fall in distinct bank
+// pairs) for one pad choice.
+static int64_t smem_wavefronts(const Plan &pl, int pad, const std::vector<int> &e_in_of_out) {
+    int64_t total = 0;
+    const int V = (int)e_in_of_out.size();
+    const int NT = pl.threads;
+    const int nwarps = std::min(NT / 32, 8);
+    for (int k = 0; k < pl.ept; ++k)
+        for (int w = 0; w < nwarps; ++w)
+            for (int h = 0; h < 2; ++h) {
+                int64_t words[16];
+                int nw = 0;
+                for (int t = 0; t < 16; ++t) {
+                    int e = k * NT + w * 32 + h * 16 + t;
+                    if (e >= V) continue;
+                    int64_t idx = e_in_of_out[e];
+                    if (pad) idx += idx / pad;
+                    words[nw++] = idx;
+                }
+                int cnt[16] = {0};
+                int worst = 0;
+                for (int a = 0; a < nw; ++a) {
+                    bool dup = false;
+                    for (int b = 0; b < a; ++b) if (words[b] == words[a]) dup = true;
+                    if (dup) continue;
+                    int bank = (int)(words[a] & 15);
+                    worst = std::max(worst, ++cnt[bank]);
+                }
+                total += worst;
+            }
+    return total;
+}
+
+int spg_plan(const Folded &fo, int op, const int *box_override, int threads_override,
+             int ept_override, int num_sms, Plan *pl) {
+    std::memset(pl, 0, sizeof(*pl));
+    pl->fo = fo;
+    pl->op = op;
+    if (fo.empty) { pl->kind = KIND_EMPTY; return SPAGHETTY_OK; }
+    const int R = fo.rank;
+    if (R <= 1 && !box_override) {
+        pl->kind = KIND_FLAT;
+        pl->threads = 256;
+        pl->ept = 8;
+        pl->run_in = pl->run_out = (int)std::min<int64_t>(fo.nelem, INT_MAX);
+        return SPAGHETTY_OK;
+    }
+    Shape s;
+    s.R = R;
+    for (int d = 0; d < R; ++d) { s.D[d] = fo.D[d]; s.in_order[d] = R - 1 - d; }
+    for (int q = 0; q < R; ++q) s.out_order[q] = fo.P[R - 1 - q];
+    int64_t L[SPG_MAXR];
+    if (box_override) {
+        for (int d = 0; d < R; ++d) {
+            if (box_override[d] < 1 || box_override[d] > s.D[d]) return SPAGHETTY_ERR_CONFIG;
+            L[d] = box_override[d];
+        }
+        int np = 0;
+        for (int d = 0; d < R; ++d) if (s.D[d] % L[d]) ++np;
+        if (np > 2) return SPAGHETTY_ERR_CONFIG;
+    } else {
+        choose_box(s, fo.nelem, num_sms, L);
+    }
+    int64_t vol = volume(s, L);
+    if (vol > kVMax) return SPAGHETTY_ERR_CONFIG;
+    for (int d = 0; d < R; ++d) pl->box[d] = (int)L[d];
+    pl->run_in = (int)run_len(s, L, s.in_order);
+    pl->run_out = (int)run_len(s, L, s.out_order);
+    // direct (no staging) only when the shared stride-1 dim alone gives
+    // coalesced rows on both sides
+    const bool same_fastest = (fo.P[R - 1] == R - 1);
+    pl->kind = (same_fastest && L[R - 1] >= kTRun) ? KIND_DIRECT : KIND_TILED;
+    if (threads_override) {
+        pl->threads = threads_override;
+        pl->ept = ept_override;
+        if (pl->threads * pl->ept < vol) return SPAGHETTY_ERR_CONFIG;
+    } else {
+        int rc = pick_block((int)vol, &pl->threads, &pl->ept);
+        if (rc) return rc;
+    }
+    return SPAGHETTY_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Kernel parameter block.
+int spg_build_params(Plan *pl, double f, double g) {
+    KParams &kp = pl->kp;
+    std::memset(&kp, 0, sizeof(kp));
+    kp.f = f;
+    kp.g = g;
+    if (pl->kind == KIND_EMPTY) return SPAGHETTY_OK;
+    if (pl->kind == KIND_FLAT) { kp.nelem = pl->fo.nelem; return SPAGHETTY_OK; }
+    const Folded &fo = pl->fo;
+    const int R = fo.rank;
+    int64_t istr[SPG_MAXR], ostr[SPG_MAXR];   // per input dim
+    int pinv[SPG_MAXR];
+    for (int q = 0; q < R; ++q) pinv[fo.P[q]] = q;
+    {
+        int64_t s = 1;
+        for (int d = R - 1; d >= 0; --d) { istr[d] = s; s *= fo.D[d]; }
+        int64_t so = 1;
+        int64_t ostr_pos[SPG_MAXR];
+        for (int q = R - 1; q >= 0; --q) { ostr_pos[q] = so; so *= fo.D[fo.P[q]]; }
+        for (int d = 0; d < R; ++d) ostr[d] = ostr_pos[pinv[d]];
+    }
+    // partial (masked) dims
+    int pA = -1, pB = -1;
+    for (int d = 0; d < R; ++d)
+        if (fo.D[d] % pl->box[d]) {
+            if (pA < 0) pA = d;
+            else if (pB < 0) pB = d;
+            else return SPAGHETTY_ERR_CONFIG;
+        }
+    pl->masked = (pA >= 0);
+    kp.lenA = pA >= 0 ? pl->box[pA] : 1;
+    kp.extA = pA >= 0 ? (int32_t)fo.D[pA] : 1;
+    kp.lenB = pB >= 0 ? pl->box[pB] : 1;
+    kp.extB = pB >= 0 ? (int32_t)fo.D[pB] : 1;
+    auto mp = [&](int d) -> int8_t { return d == pA ? 1 : (d == pB ? 2 : 0); };
+    // box-local input-order strides
+    int32_t bs[SPG_MAXR];
+    {
+        int32_t s = 1;
+        for (int d = R - 1; d >= 0; --d) { bs[d] = s; s *= pl->box[d]; }
+        kp.vol = s;
+    }
+    int64_t maxoff_in = 0, maxoff_out = 0;
+    // load walk: input order, fastest first
+    kp.ld.n = 0;
+    for (int d = R - 1; d >= 0; --d) {
+        if (pl->box[d] <= 1) continue;
+        int k = kp.ld.n++;
+        kp.ld.len[k] = make_fastdiv((uint32_t)pl->box[d]);
+        kp.ld.gs_a[k] = istr[d];
+        kp.ld.gs_b[k] = ostr[d];
+        kp.ld.bs[k] = bs[d];
+        kp.ld.mpos[k] = mp(d);
+        maxoff_in += (int64_t)(pl->box[d] - 1) * istr[d];
+        maxoff_out += (int64_t)(pl->box[d] - 1) * ostr[d];
+    }
+    // store walk: output order, fastest first
+    kp.st.n = 0;
+    for (int q = R - 1; q >= 0; --q) {
+        int d = fo.P[q];
+        if (pl->box[d] <= 1) continue;
+        int k = kp.st.n++;
+        kp.st.len[k] = make_fastdiv((uint32_t)pl->box[d]);
+        kp.st.gs_a[k] = ostr[d];
+        kp.st.gs_b[k] = istr[d];
+        kp.st.bs[k] = bs[d];
+        kp.st.mpos[k] = mp(d);
+    }
+    if (maxoff_in > INT32_MAX || maxoff_out > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
+    // grid of boxes, output order fastest first
+    int64_t ntiles = 1;
+    kp.grid.n = 0;
+    for (int q = R - 1; q >= 0; --q) {
+        int d = fo.P[q];
+        int64_t c = (fo.D[d] + pl->box[d] - 1) / pl->box[d];
+        if (c <= 1) continue;
+        int k = kp.grid.n++;
+        kp.grid.cnt[k] = make_fastdiv((uint32_t)c);
+        kp.grid.in_step[k] = (int64_t)pl->box[d] * istr[d];
+        kp.grid.out_step[k] = (int64_t)pl->box[d] * ostr[d];
+        kp.grid.mpos[k] = mp(d);
+        ntiles *= c;
+        if (c > INT32_MAX || ntiles > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
+    }
+    kp.ntiles = (uint32_t)ntiles;
+    // shared-memory padding for the tiled kernel: pick the pad period with the
+    // fewest store-phase wavefronts among {none, stride of the output-fastest
+    // box dim in the input-ordered tile}
+    kp.pad = 0;
+    if (pl->kind == KIND_TILED && kp.st.n > 0) {
+        std::vector<int> e_in(kp.vol);
+        for (int e = 0; e < kp.vol; ++e) {
+            int rem = e, lin = 0;
+            for (int k = 0; k < kp.st.n; ++k) {
+                int len = (int)kp.st.len[k].d;
+                lin += (rem % len) * kp.st.bs[k];
+                rem /= len;
+            }
+            e_in[e] = lin;
+        }
+        int cands[3] = {0, (int)kp.st.bs[0], (int)kp.st.bs[0] * 2};
+        int64_t best = -1;
+        for (int c : cands) {
+            if (c < 0 || (c && c >= kp.vol)) continue;
+            int64_t w = smem_wavefronts(*pl, c, e_in);
+            if (best < 0 || w < best) { best = w; kp.pad = c; }
+        }
+    }
+    pl->smem_bytes = pl->kind == KIND_TILED
+        ? (int)((kp.vol + (kp.pad ? kp.vol / kp.pad + 1 : 0)) * sizeof(double)) : 0;
+    return SPAGHETTY_OK;
+}
+
+// ---------------------------------------------------------------------------
+int spg_selftest_host(void) {
+    // fast division against plain division
+    uint32_t ds[] = {1, 2, 3, 5, 6, 7, 10, 12, 16, 17, 20, 29, 30, 31, 33, 100, 255,
+                     1000, 4096, 65537, 1000003, 0x7fffffffu};
+    uint32_t ns[] = {0, 1, 2, 3, 31, 32, 33, 999, 1000, 65535, 65536, 1u << 20,
+                     123456789, 0x7ffffffeu, 0x7fffffffu};
+    for (uint32_t d : ds) {
+        FastDiv f = make_fastdiv(d);
+        for (uint32_t n : ns)
+            if (fd_div(n, f) != n / d) return 1;
+        uint64_t x = 88172645463325252ull;
+        for (int t = 0; t < 20000; ++t) {
+            x ^= x << 13; x ^= x >> 7; x ^= x << 17;
+            uint32_t n = (uint32_t)(x & 0x7fffffffu);
+            if (fd_div(n, f) != n / d) return 1;
+        }
+    }
+    return 0;
+}

@@ -1,0 +1,76 @@
+"""Kernel generator: emits the compiled sm_103a variant set.
+
+The reference generates one Fortran/C loop nest per (permutation, loop order)
+and lets a tuner pick the fastest (trunk/generator2.py:48-443 emitters,
+trunk/generator2.py:446-629 tuner).  Here the search space is not the loop
+order but the shape of the staging box and the CTA that moves it, so the
+generator emits, for every arithmetic case (the generated nests' five
+(factor, acc_factor) cases, trunk/generator2.py:57-130), every kernel family
+at every (threads, elements-per-thread) point the planner and the autotuner
+may pick.  Each output file holds one arithmetic case so that the build can
+compile them in parallel; each exposes a table of (kind, op, threads, ept,
+function) entries the C-ABI dispatcher searches.
+"""
+from __future__ import annotations
+
+import os
+
+OPS = {0: "OP_COPY", 1: "OP_SCALE", 2: "OP_ACC1", 3: "OP_ACCF", 4: "OP_GEN"}
+THREADS = (128, 256, 512)
+EPTS = (1, 2, 4, 8)
+FLAT_VEC = (1, 2)
+
+HEADER = """// GENERATED by spaghetty_gb300/generator.py -- do not edit.
+// Variant table for arithmetic case {opname}.
+#include "kernels.cuh"
+"""
+
+
+def variants(op: int):
+    out = []
+    for nt in THREADS:
+        for ept in EPTS:
+            out.append(("KIND_TILED", nt, ept, "spg_tiled<%d, %d, %s>" % (nt, ept, OPS[op])))
+    for nt in THREADS:
+        for ept in EPTS:
+            out.append(("KIND_DIRECT", nt, ept, "spg_direct<%d, %d, %s>" % (nt, ept, OPS[op])))
+    for vec in FLAT_VEC:
+        out.append(("KIND_FLAT", 256, vec, "spg_flat<%s, %d>" % (OPS[op], vec)))
+    return out
+
+
+def emit_op(op: int) -> str:
+    lines = [HEADER.format(opname=OPS[op])]
+    lines.append("static const SpgKernelEntry kEntries[] = {")
+    for kind, nt, ept, fn in variants(op):
+        lines.append("    {%s, %s, %d, %d, (const void *)&%s}," % (kind, OPS[op], nt, ept, fn))
+    lines.append("};")
+    lines.append("const SpgKernelEntry *spg_kernels_op%d(int *n) {" % op)
+    lines.append("    *n = (int)(sizeof(kEntries) / sizeof(kEntries[0]));")
+    lines.append("    return kEntries;")
+    lines.append("}")
+    return "\n".join(lines) + "\n"
+
+
+def emit_all(outdir: str) -> list[str]:
+    """Write kernels_op<N>.cu for every arithmetic case; returns the paths
+    (files are rewritten only when their text changes)."""
+    paths = []
+    for op in OPS:
+        path = os.path.join(outdir, "kernels_op%d.cu" % op)
+        text = emit_op(op)
+        old = None
+        if os.path.exists(path):
+            with open(path) as fh:
+                old = fh.read()
+        if old != text:
+            with open(path, "w") as fh:
+                fh.write(text)
+        paths.append(path)
+    return paths
+
+
+if __name__ == "__main__":
+    here = os.path.join(os.path.dirname(os.path.abspath(__file__)), "csrc")
+    for p in emit_all(here):
+        print(p)

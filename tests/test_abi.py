@@ -1,0 +1,176 @@
+"""The C-ABI library on the CPU: it loads, exports every symbol the header
+declares, and its host-side logic (validation, folding, planning, index
+safety of every launch) is right.  No kernel is launched here."""
+import ctypes
+import itertools
+import os
+import random
+import re
+
+import numpy as np
+import pytest
+
+from spaghetty_gb300._lib import LIB_PATH, PROTOTYPES, int_array, lib
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                      "include", "spaghetty_gb300.h")
+
+
+def header_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    names = re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\*?\s*([a-z_][a-z0-9_]*)\s*\(",
+                       text, flags=re.M)
+    return sorted(set(names))
+
+
+def test_library_is_in_tree_and_loads():
+    assert os.path.exists(LIB_PATH)
+    assert os.path.dirname(LIB_PATH).endswith("spaghetty_gb300")
+    assert lib().spaghetty_version().startswith(b"spaghetty_gb300")
+
+
+def test_exports_every_header_symbol():
+    names = header_functions()
+    assert "tce_sort_4" in names and "tce_sortacc_6_" in names and len(names) >= 29
+    L = ctypes.CDLL(LIB_PATH)
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    # and the Python binding declares a prototype for each of them
+    assert set(names) <= set(PROTOTYPES), sorted(set(names) - set(PROTOTYPES))
+
+
+def test_host_selftest():
+    assert lib().spaghetty_selftest() == 0
+
+
+def plan(dims, perm, op=0):
+    from spaghetty_gb300 import plan as P
+    return P(dims, perm, op)
+
+
+def verify(dims, perm, op=0, sms=152):
+    st = (ctypes.c_int64 * 4)()
+    rc = lib().spaghetty_plan_verify(len(dims), int_array(dims), int_array(perm), op, sms, st)
+    return rc, list(st)
+
+
+@pytest.mark.parametrize("dims,perm,rank,kind", [
+    ((30, 30, 30, 30), (1, 2, 3, 4), 1, "flat"),
+    ((30, 30, 30, 30), (2, 1, 3, 4), 3, "direct"),
+    ((30, 30, 30, 30), (3, 4, 1, 2), 2, "tiled"),
+    ((30, 30, 30, 30), (4, 3, 2, 1), 4, "tiled"),
+    ((16,) * 6, (1, 2, 3, 4, 5, 6), 1, "flat"),
+    ((16,) * 6, (4, 5, 6, 1, 2, 3), 2, "tiled"),
+    ((1, 7, 1, 9), (3, 1, 4, 2), 2, "tiled"),
+    ((5, 1, 1, 1), (2, 3, 4, 1), 1, "flat"),
+])
+def test_folding(dims, perm, rank, kind):
+    p = plan(dims, perm)
+    assert p["rank"] == rank and p["kind"] == kind
+    assert int(np.prod(p["dims"])) == int(np.prod(dims))
+
+
+def test_plan_invariants_all_rank4_rank6():
+    cases = [((30,) * 4, p) for p in itertools.permutations((1, 2, 3, 4))]
+    cases += [((100,) * 4, p) for p in itertools.permutations((1, 2, 3, 4))]
+    cases += [((17, 29, 64, 100), p) for p in itertools.permutations((1, 2, 3, 4))]
+    cases += [((16,) * 6, p) for p in itertools.permutations(range(1, 7))]
+    cases += [((12, 20, 16, 20, 12, 16), p) for p in itertools.permutations(range(1, 7))]
+    for dims, perm in cases:
+        p = plan(dims, perm)
+        if p["kind"] == "flat":
+            continue
+        vol = int(np.prod(p["box"]))
+        assert vol <= p["threads"] * p["ept"] <= 4096, (dims, perm, p)
+        assert all(1 <= b <= d for b, d in zip(p["box"], p["dims"]))
+        # both sides get coalesced rows unless that side is shorter overall
+        total = int(np.prod(p["dims"]))
+        assert p["run_in"] >= min(32, total) and p["run_out"] >= min(32, total), (dims, perm, p)
+        npartial = sum(1 for b, d in zip(p["box"], p["dims"]) if d % b)
+        assert npartial <= 2
+
+
+def test_launch_index_safety_rank4_all_perms():
+    """Every launch the sort4 configs make is replayed on the host: reads and
+    writes in bounds, each output written once from the right input."""
+    for dims in [(3, 5, 7, 2), (1, 31, 33, 5), (30, 30, 30, 30), (17, 29, 64, 10),
+                 (8, 8, 8, 8), (40, 8, 13, 37), (2, 1, 9, 4)]:
+        for perm in itertools.permutations((1, 2, 3, 4)):
+            for op in (0, 1):
+                rc, st = verify(dims, perm, op)
+                assert rc == 0, (dims, perm, op, rc)
+
+
+def test_launch_index_safety_rank6_triples_and_random():
+    from spaghetty_gb300.workloads import TRIPLES_SORT6
+    for perm in TRIPLES_SORT6:
+        for dims in [(6, 7, 5, 6, 8, 9), (10,) * 6]:
+            rc, _ = verify(dims, perm, 1)
+            assert rc == 0, (dims, perm)
+    rnd = random.Random(3)
+    for _ in range(200):
+        r = rnd.choice([2, 3, 5, 6, 7, 8])
+        dims = [rnd.randint(1, 40 if r <= 3 else 9) for _ in range(r)]
+        if np.prod(dims) > 3e6:
+            continue
+        perm = list(range(1, r + 1))
+        rnd.shuffle(perm)
+        rc, _ = verify(dims, perm, rnd.randint(0, 2), rnd.choice([1, 8, 152]))
+        assert rc == 0, (dims, perm)
+
+
+@pytest.mark.parametrize("perm,code", [((1, 1, 2, 3), 2), ((0, 1, 2, 3), 2), ((1, 2, 3, 5), 2)])
+def test_bad_permutation_status(perm, code):
+    from tests._util import call_status
+    u = np.zeros(16)
+    s = np.zeros(16)
+    rc = call_status("tce_sort_4_status", u.ctypes.data, s.ctypes.data, (2, 2, 2, 2), perm, 1.0)
+    assert rc == code
+    assert lib().spaghetty_last_error() == code
+
+
+def test_negative_dim_and_empty():
+    from tests._util import call_status
+    u = np.zeros(4)
+    s = np.zeros(4)
+    assert call_status("tce_sort_4_status", u.ctypes.data, s.ctypes.data,
+                       (2, -1, 2, 1), (1, 2, 3, 4), 1.0) == 3
+    # a zero extent is an empty tensor: nothing to do, like the reference's
+    # zero-trip loops
+    assert call_status("tce_sort_4_status", u.ctypes.data, s.ctypes.data,
+                       (2, 0, 2, 1), (4, 3, 2, 1), 1.0) == 0
+
+
+def test_void_dropin_prints_reference_diagnostic(capfd):
+    from tests._util import call_dropin
+    u = np.zeros(16)
+    s = np.full(16, 7.0)
+    call_dropin("tce_sort_4", u.ctypes.data, s.ctypes.data, (2, 2, 2, 2), (1, 2, 2, 4), 1.0)
+    err = capfd.readouterr().err
+    assert "something is wrong" in err
+    assert np.all(s == 7.0)  # output untouched
+    assert lib().spaghetty_last_error() == 2
+
+
+def test_alias_rejected():
+    from tests._util import call_status
+    buf = np.zeros(32)
+    rc = call_status("tce_sort_4_status", buf.ctypes.data, buf.ctypes.data + 8 * 4,
+                     (2, 2, 2, 2), (4, 3, 2, 1), 1.0)
+    assert rc == 6
+
+
+def test_tune_set_validation():
+    L = lib()
+    d = int_array((30, 30, 30, 30))
+    p = int_array((4, 3, 2, 1))
+    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 30)), 128, 8) == 9  # too small
+    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 31)), 512, 8) == 9  # > extent
+    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 30)), 512, 8) == 0
+    assert plan((30, 30, 30, 30), (4, 3, 2, 1))["box"] == [30, 2, 2, 30]
+    assert L.spaghetty_tune_set(4, d, p, 0, int_array((15, 1, 1, 15)), 256, 1) == 0
+    assert plan((30, 30, 30, 30), (4, 3, 2, 1))["box"] == [15, 1, 1, 15]
+    assert verify((30, 30, 30, 30), (4, 3, 2, 1))[0] == 0
+    assert L.spaghetty_tune_set(0, None, None, 0, None, 0, 0) == 0   # clear
+    assert plan((30, 30, 30, 30), (4, 3, 2, 1))["box"] != [15, 1, 1, 15]

@@ -1,0 +1,288 @@
+"""GPU parity: the CUDA kernels, called through the C ABI, against the
+reference (golden digests made by the reference's own nests) and the oracle,
+bit for bit.  Shapes are the sort4/sort6 configurations and the edge cases
+the reference's tester covers (trunk/generator2.py:446-629: every
+permutation, factors 1 and 37, the init_4d_array fixture), plus odd
+extents, unit dims, misaligned buffers and guard bands."""
+import ctypes
+import itertools
+import random
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spaghetty_gb300 import sort_generic
+from spaghetty_gb300._lib import int_array, lib
+from spaghetty_gb300.workloads import TRIPLES_SORT6
+from tests._util import (bits_equal, call_dropin, first_mismatch, golden, golden_inputs,
+                         parse_key)
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def dev(a, cuda):
+    return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64)).to(cuda)
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.cpu().numpy()
+
+
+def gpu_sort(u, dims, perm, f, g, y0, cuda, via="dropin"):
+    """Run one sort on the GPU through the C ABI; returns the output (numpy)."""
+    du = dev(u, cuda)
+    ds = dev(y0, cuda) if g else torch.zeros(du.numel(), dtype=torch.float64, device=cuda)
+    torch.cuda.synchronize()
+    if via == "dropin" and g in (0.0, 1.0) and len(dims) in (2, 4, 6, 8):
+        name = "tce_sort%s_%d" % ("acc" if g else "", len(dims))
+        call_dropin(name, du.data_ptr(), ds.data_ptr(), dims, perm, f)
+        assert lib().spaghetty_last_error() == 0
+    else:
+        sort_generic(du, ds, dims, perm, f, g)
+    return host(ds)
+
+
+def check(got, want, what):
+    if not bits_equal(got, want):
+        pytest.fail("%s: mismatch %s" % (what, first_mismatch(got, want)))
+
+
+# ---------------------------------------------------------------------------
+def test_golden_digests_all_perms(cuda):
+    """All 4032 golden cases (24 rank-4 and 720 rank-6 permutations, sort and
+    sortacc, factors 1, -1, 37, +-0.5, integer fixture) reproduce the
+    reference nests' output digests."""
+    bad = []
+    for key, digest in golden().items():
+        dims, inp, perm, f, g = parse_key(key)
+        u, s0 = golden_inputs(dims, inp)
+        out = gpu_sort(u, dims, perm, f, g, s0, cuda)
+        if O.digest(out)[:16] != digest:
+            bad.append(key)
+    assert not bad, bad[:10]
+
+
+@pytest.mark.parametrize("acc", [False, True])
+def test_sort4_plain_30(cuda, acc):
+    """configs[0]: 30^4, b(i,j,k,l) = f*a(l,k,j,i), f = -0.5, every perm."""
+    dims = (30, 30, 30, 30)
+    n = 30 ** 4
+    u = O.seeded_uniform(n, 1)
+    y = O.seeded_uniform(n, 2)
+    for perm in itertools.permutations((1, 2, 3, 4)):
+        want = O.np_sort(u, dims, perm, -0.5, 1.0 if acc else 0.0, out=y)
+        got = gpu_sort(u, dims, perm, -0.5, 1.0 if acc else 0.0, y, cuda)
+        check(got, want, ("sort4", perm, acc))
+    # and against the scalar C restatement of old_sort_4 for the headline perm
+    want = O.old_sort(u, dims, (4, 3, 2, 1), -0.5, out=(y.copy() if acc else None), acc=acc)
+    got = gpu_sort(u, dims, (4, 3, 2, 1), -0.5, 1.0 if acc else 0.0, y, cuda)
+    check(got, want, "old_sort_4 4321")
+
+
+@pytest.mark.parametrize("dims", [(20, 20, 20, 20), (50, 50, 50, 50), (17, 29, 64, 100)])
+def test_sort4_sweep_sizes(cuda, dims):
+    n = int(np.prod(dims))
+    u = O.seeded_uniform(n, 3)
+    y = O.seeded_uniform(n, 4)
+    for perm in itertools.permutations((1, 2, 3, 4)):
+        for f in (1.0, -1.0, 0.5):
+            for g in (0.0, 1.0):
+                want = O.np_sort(u, dims, perm, f, g, out=y)
+                got = gpu_sort(u, dims, perm, f, g, y, cuda)
+                check(got, want, (dims, perm, f, g))
+
+
+def test_sort4_100_full_size(cuda):
+    """100^4 (800 MB per tensor): oracle parity for two perms, and for every
+    perm the round trip sort(p) then sort(p^-1) restores the input exactly
+    (factor 0.5 then 2: exact power-of-two scalings)."""
+    dims = (100,) * 4
+    n = 100 ** 4
+    g = torch.Generator(device=cuda)
+    g.manual_seed(7)
+    u = torch.rand(n, dtype=torch.float64, device=cuda, generator=g) * 2 - 1
+    s = torch.empty_like(u)
+    r = torch.empty_like(u)
+    for perm in itertools.permutations((1, 2, 3, 4)):
+        inv = [0] * 4
+        for q, p in enumerate(perm):
+            inv[p - 1] = q + 1
+        sd = tuple(dims[p - 1] for p in perm)
+        sort_generic(u, s, dims, perm, 0.5, 0.0)
+        sort_generic(s, r, sd, inv, 2.0, 0.0)
+        torch.cuda.synchronize()
+        assert torch.equal(r, u), perm
+    uh = u.cpu().numpy()
+    yh = O.seeded_uniform(n, 9)
+    for perm in [(4, 3, 2, 1), (2, 4, 1, 3)]:
+        for gfac in (0.0, 1.0):
+            want = O.np_sort(uh, dims, perm, -0.5, gfac, out=yh)
+            got = gpu_sort(uh, dims, perm, -0.5, gfac, yh, cuda, via="generic")
+            check(got, want, ("100^4", perm, gfac))
+
+
+def test_sort6_all_perms_10(cuda):
+    dims = (10,) * 6
+    n = 10 ** 6
+    u = O.seeded_uniform(n, 5)
+    y = O.seeded_uniform(n, 6)
+    for i, perm in enumerate(itertools.permutations(range(1, 7))):
+        g = float(i % 2)
+        want = O.np_sort(u, dims, perm, -0.5, g, out=y)
+        got = gpu_sort(u, dims, perm, -0.5, g, y, cuda)
+        check(got, want, ("sort6 10^6", perm, g))
+
+
+def test_sort6_triples_16(cuda):
+    dims = (16,) * 6
+    n = 16 ** 6
+    u = O.seeded_uniform(n, 7)
+    y = O.seeded_uniform(n, 8)
+    for perm in TRIPLES_SORT6:
+        for g in (0.0, 1.0):
+            want = O.np_sort(u, dims, perm, 1.0 if g else -0.5, g, out=y)
+            got = gpu_sort(u, dims, perm, 1.0 if g else -0.5, g, y, cuda)
+            check(got, want, ("sort6 16^6", perm, g))
+
+
+def test_sort6_noncubic_and_20(cuda):
+    rnd = random.Random(11)
+    perms = rnd.sample(list(itertools.permutations(range(1, 7))), 24)
+    dims = (12, 20, 16, 20, 12, 16)
+    n = int(np.prod(dims))
+    u = O.seeded_uniform(n, 9)
+    y = O.seeded_uniform(n, 10)
+    for perm in perms:
+        for g in (0.0, 1.0):
+            want = O.np_sort(u, dims, perm, 0.5, g, out=y)
+            got = gpu_sort(u, dims, perm, 0.5, g, y, cuda)
+            check(got, want, ("sort6 noncubic", perm, g))
+    # 20^6 = 64M elements: round trip on the device for a few perms
+    dims = (20,) * 6
+    gen = torch.Generator(device=cuda)
+    gen.manual_seed(3)
+    du = torch.rand(20 ** 6, dtype=torch.float64, device=cuda, generator=gen) - 0.5
+    s = torch.empty_like(du)
+    r = torch.empty_like(du)
+    for perm in [(6, 5, 4, 3, 2, 1), (2, 6, 1, 5, 4, 3), (4, 5, 6, 1, 2, 3)]:
+        inv = [0] * 6
+        for q, p in enumerate(perm):
+            inv[p - 1] = q + 1
+        sort_generic(du, s, dims, perm, -1.0, 0.0)
+        sort_generic(s, r, dims, inv, -1.0, 0.0)
+        torch.cuda.synchronize()
+        assert torch.equal(r, du), perm
+
+
+def test_odd_extents_and_unit_dims(cuda):
+    rnd = random.Random(5)
+    ext = [1, 2, 3, 5, 7, 31, 33]
+    for it in range(120):
+        r = rnd.choice([2, 3, 4, 5, 6, 7, 8])
+        dims = tuple(rnd.choice(ext) for _ in range(r))
+        if np.prod(dims) > 2_000_000:
+            continue
+        perm = list(range(1, r + 1))
+        rnd.shuffle(perm)
+        n = int(np.prod(dims))
+        u = O.fixture_values(n, it)
+        y = O.fixture_values(n, 500 + it)
+        f = rnd.choice([1.0, -1.0, 0.3, 37.0])
+        g = rnd.choice([0.0, 1.0, -2.5])
+        want = O.np_sort(u, dims, perm, f, g, out=y)
+        got = gpu_sort(u, dims, perm, f, g, y, cuda, via="generic")
+        check(got, want, (dims, perm, f, g))
+
+
+def test_rank2_rank8_dropins(cuda):
+    for dims, perm in [((33, 65), (2, 1)), ((3, 2, 4, 3, 2, 5, 2, 3), (8, 1, 7, 2, 6, 3, 5, 4))]:
+        n = int(np.prod(dims))
+        u = O.fixture_values(n, 40)
+        y = O.fixture_values(n, 41)
+        for g in (0.0, 1.0):
+            want = O.old_sort(u, dims, perm, 0.25, out=(y.copy() if g else None), acc=bool(g))
+            got = gpu_sort(u, dims, perm, 0.25, g, y, cuda)
+            check(got, want, (dims, perm, g))
+
+
+def test_guard_bands_and_misaligned_buffers(cuda):
+    """Outputs written exactly in place: canaries around the output stay
+    untouched, including buffers offset by one double (no 16-byte alignment)."""
+    G = 37
+    canary = -12345.678
+    for dims, perm in [((30, 30, 30, 30), (1, 2, 3, 4)), ((30, 30, 30, 30), (4, 3, 2, 1)),
+                       ((17, 29, 64, 10), (2, 1, 3, 4)), ((7, 3, 5), (3, 1, 2))]:
+        n = int(np.prod(dims))
+        for off in (0, 1):
+            u = O.fixture_values(n, 60)
+            y = O.fixture_values(n, 61)
+            bu = torch.full((n + 2 * G,), canary, dtype=torch.float64, device=cuda)
+            bs = torch.full((n + 2 * G,), canary, dtype=torch.float64, device=cuda)
+            vu = bu[G + off:G + off + n]
+            vs = bs[G + off:G + off + n]
+            vu.copy_(torch.from_numpy(u))
+            vs.copy_(torch.from_numpy(y))
+            for g in (0.0, 1.0):
+                vs.copy_(torch.from_numpy(y))
+                sort_generic(vu, vs, dims, perm, -0.5, g)
+                got = host(vs)
+                check(got, O.np_sort(u, dims, perm, -0.5, g, out=y), (dims, perm, off, g))
+                b = host(bs)
+                assert np.all(b[:G + off] == canary) and np.all(b[G + off + n:] == canary)
+
+
+def test_host_buffers_are_staged(cuda):
+    """The drop-ins accept host pointers (pageable numpy and pinned torch)."""
+    dims = (17, 29, 64, 10)
+    n = int(np.prod(dims))
+    u = O.fixture_values(n, 70)
+    y = O.fixture_values(n, 71)
+    for perm in [(4, 3, 2, 1), (1, 2, 3, 4), (2, 1, 3, 4)]:
+        s = np.zeros(n)
+        call_dropin("tce_sort_4", u.ctypes.data, s.ctypes.data, dims, perm, -0.5)
+        assert lib().spaghetty_last_error() == 0
+        check(s, O.np_sort(u, dims, perm, -0.5), ("host sort", perm))
+        s = y.copy()
+        call_dropin("tce_sortacc_4", u.ctypes.data, s.ctypes.data, dims, perm, 37.0)
+        check(s, O.np_sort(u, dims, perm, 37.0, 1.0, out=y), ("host sortacc", perm))
+        pu = torch.from_numpy(u).pin_memory()
+        ps = torch.from_numpy(y).pin_memory()
+        call_dropin("tce_sortacc_4", pu.data_ptr(), ps.data_ptr(), dims, perm, 0.5)
+        check(ps.numpy(), O.np_sort(u, dims, perm, 0.5, 1.0, out=y), ("pinned", perm))
+        # mixed: device input, host output
+        du = dev(u, cuda)
+        s = np.zeros(n)
+        call_dropin("tce_sort_4", du.data_ptr(), s.ctypes.data, dims, perm, 1.0)
+        check(s, O.np_sort(u, dims, perm, 1.0), ("mixed", perm))
+
+
+def test_async_on_side_stream(cuda):
+    dims = (30, 30, 30, 30)
+    n = 30 ** 4
+    u = O.seeded_uniform(n, 80)
+    du = dev(u, cuda)
+    ds = torch.empty_like(du)
+    st = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(st):
+        rc = lib().spaghetty_sort_async(4, ctypes.c_void_p(du.data_ptr()),
+                                        ctypes.c_void_p(ds.data_ptr()), int_array(dims),
+                                        int_array((3, 1, 4, 2)), -0.5, 0.0,
+                                        ctypes.c_void_p(st.cuda_stream))
+        assert rc == 0
+    st.synchronize()
+    check(ds.cpu().numpy(), O.np_sort(u, dims, (3, 1, 4, 2), -0.5), "side stream")
+
+
+def test_status_form_bad_perm_leaves_output(cuda):
+    from tests._util import call_status
+    du = torch.zeros(16, dtype=torch.float64, device=cuda)
+    ds = torch.full((16,), 3.0, dtype=torch.float64, device=cuda)
+    rc = call_status("tce_sort_4_status", du.data_ptr(), ds.data_ptr(), (2, 2, 2, 2),
+                     (2, 2, 3, 4), 1.0)
+    assert rc == 2
+    assert torch.all(ds == 3.0)
