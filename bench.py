@@ -421,8 +421,44 @@ def run_reference(args, ws, rank):
     }
 
 
+def run_case(args):
+    """One sort case, W warm-up + K timed launches (the profiling workload)."""
+    import torch
+    import spaghetty_gb300 as S
+    dims_s, perm_s, op_s = args.case.split(":")
+    dims = tuple(int(x) for x in dims_s.split(","))
+    perm = tuple(int(x) for x in perm_s.split(","))
+    op = int(op_s)
+    n = 1
+    for d in dims:
+        n *= d
+    dev = torch.device("cuda", 0)
+    u = torch.rand(n, dtype=torch.float64, device=dev)
+    s = torch.rand(n, dtype=torch.float64, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    g = 0.0 if op == 0 else 1.0
+    times = []
+    for r in range(args.warmup + args.steps):
+        if n * 16 < 2 * L2_BYTES:
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        S.sort_generic(u, s, dims, perm, 0.5, g)
+        e1.record()
+        e1.synchronize()
+        if r >= args.warmup:
+            times.append(e0.elapsed_time(e1))
+    ms = statistics.median(times)
+    b = case_bytes(dims, op == 1)
+    print(json.dumps({"case": args.case, "ms": round(ms, 4), "gbs": round(b / ms / 1e6, 1),
+                      "plan": S.plan(dims, perm, op)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default=None,
+                    help="dims:perm:op (op 0 sort, 1 sortacc): time one case only")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -432,6 +468,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     ws, rank, local = dist_env()
+    if args.case:
+        run_case(args)
+        return
     if args.impl == "reference":
         line = run_reference(args, ws, rank)
         if line is not None:

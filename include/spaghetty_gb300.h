@@ -188,6 +188,8 @@ typedef struct spaghetty_plan_info {
     int masked;         /* 1 when boundary boxes need element masks      */
     int grid;           /* CTAs launched                                  */
     int vec;            /* 2 when 16-byte vector accesses are used        */
+    int stages;         /* tiled: 0 = register-staged, 2/3 = cp.async pipeline depth */
+    int smem_bytes;     /* dynamic shared memory per CTA                  */
 } spaghetty_plan_info;
 
 /* Fold and plan without launching.  op: 0 = sort, 1 = sortacc, 2 = general
@@ -208,10 +210,21 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
 
 /* Autotuner hook: force the tile box / block shape for subsequent calls
  * with the same folded (dims, perm, op).  box[] is indexed by folded dim;
- * threads in {128,256,512}; ept in {1,2,4,8}.  Pass box == NULL to clear
- * every override.  Returns a SPAGHETTY_* code. */
+ * threads in {128,256,512}; ept in {1,2,4,8}; stages in {0,2,3} (tiled
+ * kernel: 0 = register-staged, 2/3 = cp.async pipeline depth, needs
+ * ept >= 2).  Pass box == NULL to clear every override.  Returns a
+ * SPAGHETTY_* code. */
 int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op,
-                       const int *box, int threads, int ept);
+                       const int *box, int threads, int ept, int stages);
+
+/* Load autotuner winners from a tune file (lines
+ * `gpu_name|sm_count|folded dims|folded perm (0-based)|op class|box|threads|ept|stages`)
+ * for the current device; returns how many were installed, or -1 if the
+ * file cannot be read.  The library also loads, once, the file named by
+ * $SPAGHETTY_GB300_TUNE_FILE (empty = none), else tune_cache.txt beside the
+ * shared library -- the per-GPU table the reference shipped as makelib's
+ * best-loop list (trunk/makelib.py:39-62). */
+int spaghetty_tune_load(const char *path);
 
 /* Host-side self checks of the planner's integer helpers (fast division by
  * invariant divisors).  Returns 0 when they pass.  Needs no GPU. */

@@ -36,6 +36,8 @@ class PlanInfo(ctypes.Structure):
         ("masked", ctypes.c_int),
         ("grid", ctypes.c_int),
         ("vec", ctypes.c_int),
+        ("stages", ctypes.c_int),
+        ("smem_bytes", ctypes.c_int),
     ]
 
 
@@ -66,9 +68,10 @@ PROTOTYPES = {
     "spaghetty_plan_query": (ctypes.c_int, [ctypes.c_int, c_int_p, c_int_p, ctypes.c_int,
                                             ctypes.POINTER(PlanInfo)]),
     "spaghetty_tune_set": (ctypes.c_int, [ctypes.c_int, c_int_p, c_int_p, ctypes.c_int,
-                                          c_int_p, ctypes.c_int, ctypes.c_int]),
+                                          c_int_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "spaghetty_plan_verify": (ctypes.c_int, [ctypes.c_int, c_int_p, c_int_p, ctypes.c_int,
                                              ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
+    "spaghetty_tune_load": (ctypes.c_int, [ctypes.c_char_p]),
     "spaghetty_selftest": (ctypes.c_int, []),
     "spaghetty_version": (ctypes.c_char_p, []),
 }

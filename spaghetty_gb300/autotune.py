@@ -1,0 +1,317 @@
+"""Brute-force autotuner with a persistent cache.
+
+The reference times every loop order of a permutation and keeps the fastest
+(trunk/generator2.py:581-622; "best" and "good within 1.2x" rows), then bakes
+the winners into a dispatch table (trunk/makelib.py:39-62, the `knight`
+table).  Here the search space is the staging box (how much of each folded
+index one CTA moves), the CTA shape (threads x elements per thread) and the
+pipeline depth of the tiled kernel; the winners are stored in a JSON cache
+keyed by (GPU, folded dims, folded permutation, operation class) and pushed
+into the library with spaghetty_tune_set().  Tuning resumes by skipping keys
+already in the cache.
+
+CLI:  python -m spaghetty_gb300.autotune --sweep sort4 [--cache FILE]
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import itertools
+import json
+import os
+import time
+from typing import Sequence
+
+from ._lib import int_array, lib
+from .sort import plan
+
+DEFAULT_CACHE = os.environ.get(
+    "SPAGHETTY_GB300_TUNE_CACHE",
+    os.path.join(os.path.dirname(os.path.abspath(__file__)), "tune_cache.json"))
+
+THREADS = (128, 256, 512)
+EPTS = (1, 2, 4, 8)
+VMAX = 4096
+
+
+def _split_len(D: int, want: int) -> int:
+    if want >= D:
+        return D
+    want = max(1, want)
+    nt = max(1, D // want)
+    return -(-D // nt)
+
+
+def _run(L, D, order):
+    r = 1
+    for d in order:
+        r *= L[d]
+        if L[d] < D[d]:
+            break
+    return r
+
+
+def _frontier(L, D, order):
+    for d in order:
+        if L[d] < D[d]:
+            return d
+    return -1
+
+
+def greedy_box(D: Sequence[int], P: Sequence[int], trun_in: int, trun_out: int,
+               vtarget: int) -> list[int]:
+    """The planner's greedy box (plan.cpp choose_box) with free targets."""
+    R = len(D)
+    L = [1] * R
+    in_order = list(range(R - 1, -1, -1))
+    out_order = [P[q] for q in range(R - 1, -1, -1)]
+    for _ in range(64):
+        vol = 1
+        for x in L:
+            vol *= x
+        ri, ro = _run(L, D, in_order), _run(L, D, out_order)
+        if ri < trun_in and _frontier(L, D, in_order) >= 0:
+            d = _frontier(L, D, in_order)
+            need = -(-trun_in * L[d] // ri)
+        elif ro < trun_out and _frontier(L, D, out_order) >= 0:
+            d = _frontier(L, D, out_order)
+            need = -(-trun_out * L[d] // ro)
+        else:
+            break
+        nl = _split_len(D[d], need)
+        if vol // L[d] * nl > VMAX:
+            nl = max(L[d], VMAX * L[d] // vol)
+        if nl <= L[d]:
+            break
+        L[d] = nl
+    for _ in range(64):
+        vol = 1
+        for x in L:
+            vol *= x
+        if vol >= vtarget:
+            break
+        ri, ro = _run(L, D, in_order), _run(L, D, out_order)
+        fi, fo = _frontier(L, D, in_order), _frontier(L, D, out_order)
+        if fi >= 0 and fo >= 0:
+            d = fo if ro <= ri else fi
+        else:
+            d = fo if fo >= 0 else fi
+        if d < 0:
+            break
+        want = min(L[d] * 2, L[d] * max(2, vtarget // vol))
+        nl = _split_len(D[d], want)
+        if vol // L[d] * nl > VMAX:
+            break
+        if nl <= L[d]:
+            break
+        L[d] = nl
+    # at most two partial dims: round others down to divisors
+    fi, fo = _frontier(L, D, in_order), _frontier(L, D, out_order)
+    for d in range(R):
+        if L[d] < D[d] and D[d] % L[d] and d not in (fi, fo):
+            x = L[d]
+            while x > 1 and D[d] % x:
+                x -= 1
+            L[d] = x
+    return L
+
+
+def candidates(dims: Sequence[int], perm: Sequence[int], op: int = 0):
+    """Candidate (box, threads, ept, stages) for one problem."""
+    p = plan(dims, perm, op)
+    if p["kind"] == "flat":
+        return p, []
+    D, P = p["dims"], p["perm"]
+    boxes = []
+    for ti, to, vt in itertools.product((16, 32, 64), (16, 32, 64), (512, 1024, 2048, 4096)):
+        b = greedy_box(D, P, ti, to, vt)
+        if b not in boxes:
+            boxes.append(b)
+    out = []
+    for b in boxes:
+        vol = 1
+        for x in b:
+            vol *= x
+        if vol > VMAX:
+            continue
+        for nt, ept in itertools.product(THREADS, EPTS):
+            cap = nt * ept
+            if cap < vol or cap >= 2 * vol + nt:
+                continue
+            stages = (0,) if (p["kind"] == "direct" or ept < 2) else (0, 2, 3)
+            for st in stages:
+                out.append((list(b), nt, ept, st))
+    return p, out
+
+
+def _set(dims, perm, op, cfg):
+    box, nt, ept, st = cfg
+    return lib().spaghetty_tune_set(len(dims), int_array(dims), int_array(perm), op,
+                                    int_array(box), nt, ept, st)
+
+
+def clear():
+    lib().spaghetty_tune_set(0, None, None, 0, None, 0, 0, 0)
+
+
+def time_case(dims, perm, op, reps=5, device=None, flush_bytes=512 << 20, bufs=None):
+    """Median kernel time (s) of one sort on device buffers, L2 flushed
+    before every launch when the tensors are smaller than 2x L2."""
+    import torch
+    from .sort import sort_generic
+    dev = device or torch.device("cuda", torch.cuda.current_device())
+    n = 1
+    for d in dims:
+        n *= d
+    if bufs is None:
+        u = torch.rand(n, dtype=torch.float64, device=dev)
+        s = torch.rand(n, dtype=torch.float64, device=dev)
+    else:
+        u, s = bufs
+    flush = torch.empty(flush_bytes // 4, dtype=torch.float32, device=dev)
+    g = 0.0 if op == 0 else (1.0 if op == 1 else 2.0)
+    times = []
+    for r in range(reps + 1):
+        if n * 16 < 2 * 129 * 1024 * 1024:
+            flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        sort_generic(u, s, dims, perm, 0.5, g)
+        e1.record()
+        e1.synchronize()
+        if r:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    times.sort()
+    return times[len(times) // 2]
+
+
+def gpu_key():
+    import torch
+    pr = torch.cuda.get_device_properties(torch.cuda.current_device())
+    return "%s/%dsm" % (pr.name, pr.multi_processor_count)
+
+
+def problem_key(p, op):
+    cls = 0 if op == 0 else (1 if op == 1 else 2)
+    return "%s|%s|%d" % (",".join(map(str, p["dims"])), ",".join(map(str, p["perm"])), cls)
+
+
+def load_cache(path=DEFAULT_CACHE) -> dict:
+    try:
+        with open(path) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+def save_cache(cache: dict, path=DEFAULT_CACHE):
+    """Write the JSON cache and, beside it, the line format the C library
+    loads by itself (tune_cache.txt next to the shared library)."""
+    tmp = path + ".tmp%d" % os.getpid()
+    with open(tmp, "w") as fh:
+        json.dump(cache, fh, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+    txt = os.path.splitext(path)[0] + ".txt"
+    lines = ["# gpu|sms|folded dims|folded perm (0-based)|op class|box|threads|ept|stages"]
+    for gk, ents in sorted(cache.items()):
+        name, sms = gk.rsplit("/", 1)
+        for key, e in sorted(ents.items()):
+            d, p, cls = key.split("|")
+            lines.append("|".join([name, sms.rstrip("sm"), d, p, cls,
+                                   ",".join(map(str, e["box"])), str(e["threads"]),
+                                   str(e["ept"]), str(e["stages"])]))
+    with open(txt + ".tmp", "w") as fh:
+        fh.write("\n".join(lines) + "\n")
+    os.replace(txt + ".tmp", txt)
+
+
+def apply_cache(cache: dict | None = None, gpu: str | None = None) -> int:
+    """Push every cached winner for this GPU into the library."""
+    cache = load_cache() if cache is None else cache
+    gpu = gpu or gpu_key()
+    nset = 0
+    for key, ent in cache.get(gpu, {}).items():
+        dims_s, perm_s, cls = key.split("|")
+        D = [int(x) for x in dims_s.split(",")]
+        # the folded problem itself is a valid (dims, perm) call: perm 1-based
+        P1 = [int(x) + 1 for x in perm_s.split(",")]
+        rc = _set(D, P1, int(cls), (ent["box"], ent["threads"], ent["ept"], ent["stages"]))
+        nset += rc == 0
+    return nset
+
+
+def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False):
+    """Time every candidate for (dims, perm, op); store and apply the best."""
+    import torch
+    p, cands = candidates(dims, perm, op)
+    if not cands:
+        return None
+    cache = load_cache() if cache is None else cache
+    gk = gpu_key()
+    key = problem_key(p, op)
+    if not force and key in cache.get(gk, {}):
+        return cache[gk][key]
+    n = 1
+    for d in dims:
+        n *= d
+    dev = torch.device("cuda", torch.cuda.current_device())
+    bufs = (torch.rand(n, dtype=torch.float64, device=dev),
+            torch.rand(n, dtype=torch.float64, device=dev))
+    clear()
+    t_default = time_case(dims, perm, op, reps, bufs=bufs)
+    results = []
+    for cfg in cands:
+        if _set(dims, perm, op, cfg) != 0:
+            continue
+        try:
+            t = time_case(dims, perm, op, reps, bufs=bufs)
+        except Exception:
+            continue
+        results.append((t, cfg))
+    clear()
+    if not results:
+        return None
+    results.sort(key=lambda r: r[0])
+    t, (box, nt, ept, st) = results[0]
+    bpe = 16 if op == 0 else 24
+    ent = {"box": box, "threads": nt, "ept": ept, "stages": st, "seconds": t,
+           "gbs": n * bpe / t / 1e9, "default_seconds": t_default,
+           "default_gbs": n * bpe / t_default / 1e9, "candidates": len(results),
+           "good": sum(1 for r in results if r[0] < 1.2 * t)}
+    if verbose:
+        print(json.dumps({"dims": list(dims), "perm": list(perm), "op": op, **ent}), flush=True)
+    cache.setdefault(gk, {})[key] = ent
+    return ent
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--sweep", default="sort4", choices=["sort4", "sort6-triples", "case"])
+    ap.add_argument("--dims", default="100,100,100,100")
+    ap.add_argument("--perm", default="4,3,2,1")
+    ap.add_argument("--ops", default="0,1")
+    ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--cache", default=DEFAULT_CACHE)
+    ap.add_argument("--force", action="store_true")
+    args = ap.parse_args()
+    from .workloads import PERMS4, SORT4_DIMS, TRIPLES_SORT6
+    ops = [int(x) for x in args.ops.split(",")]
+    if args.sweep == "sort4":
+        probs = [(d, p) for d in SORT4_DIMS for p in PERMS4]
+    elif args.sweep == "sort6-triples":
+        probs = [((16,) * 6, p) for p in TRIPLES_SORT6]
+    else:
+        probs = [(tuple(int(x) for x in args.dims.split(",")),
+                  tuple(int(x) for x in args.perm.split(",")))]
+    cache = load_cache(args.cache)
+    t0 = time.time()
+    for dims, perm in probs:
+        for op in ops:
+            tune(dims, perm, op, args.reps, cache, verbose=True, force=args.force)
+        save_cache(cache, args.cache)
+    print("tuned %d problems in %.1fs" % (len(probs) * len(ops), time.time() - t0))
+
+
+if __name__ == "__main__":
+    main()

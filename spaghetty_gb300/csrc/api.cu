@@ -10,8 +10,10 @@
 #include "plan.h"
 
 #include <cuda_runtime.h>
+#include <dlfcn.h>
 
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <mutex>
@@ -37,13 +39,13 @@ std::mutex g_mu;
 
 struct TuneOverride {
     int box[SPG_MAXR];
-    int threads, ept;
+    int threads, ept, stages;
 };
 std::map<std::string, TuneOverride> g_tune;
 std::map<int, int> g_sms;
 std::map<std::pair<const void *, int>, int> g_occ;
 
-const SpgKernelEntry *find_kernel(int kind, int op, int nt, int ept) {
+const SpgKernelEntry *find_kernel(int kind, int op, int nt, int ept, int stages) {
     static const SpgKernelEntry *tabs[OP_COUNT];
     static int counts[OP_COUNT];
     static std::once_flag once;
@@ -57,7 +59,7 @@ const SpgKernelEntry *find_kernel(int kind, int op, int nt, int ept) {
     if (op < 0 || op >= OP_COUNT) return nullptr;
     for (int i = 0; i < counts[op]; ++i) {
         const SpgKernelEntry &e = tabs[op][i];
-        if (e.kind == kind && e.threads == nt && e.ept == ept) return &e;
+        if (e.kind == kind && e.threads == nt && e.ept == ept && e.stages == stages) return &e;
     }
     return nullptr;
 }
@@ -100,7 +102,10 @@ std::string tune_key(const Folded &fo, int op) {
     return k;
 }
 
+void autoload_tune_file();
+
 int make_plan(int rank, const int *dims, const int *perm, double f, double g, int sms, Plan *pl) {
+    autoload_tune_file();
     Folded fo;
     int rc = spg_fold(rank, dims, perm, &fo);
     if (rc) return rc;
@@ -112,8 +117,8 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
         auto it = g_tune.find(tune_key(fo, op));
         if (it != g_tune.end()) { ov = it->second; have = true; }
     }
-    rc = have ? spg_plan(fo, op, ov.box, ov.threads, ov.ept, sms, pl)
-              : spg_plan(fo, op, nullptr, 0, 0, sms, pl);
+    rc = have ? spg_plan(fo, op, ov.box, ov.threads, ov.ept, ov.stages, sms, pl)
+              : spg_plan(fo, op, nullptr, 0, 0, 0, sms, pl);
     if (rc) return rc;
     return spg_build_params(pl, f, g);
 }
@@ -126,7 +131,7 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
     cudaError_t err;
     if (pl.kind == KIND_FLAT) {
         const int vec = (aligned16(u) && aligned16(s)) ? 2 : 1;
-        const SpgKernelEntry *k = find_kernel(KIND_FLAT, pl.op, 256, vec);
+        const SpgKernelEntry *k = find_kernel(KIND_FLAT, pl.op, 256, vec, 0);
         if (!k) return SPAGHETTY_ERR_NOKERNEL;
         int64_t n = pl.fo.nelem;
         int64_t work = (n / vec + 255) / 256;
@@ -136,7 +141,7 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
         pl.grid = grid;
         err = cudaLaunchKernel(k->fn, dim3(grid), dim3(256), args, 0, st);
     } else {
-        const SpgKernelEntry *k = find_kernel(pl.kind, pl.op, pl.threads, pl.ept);
+        const SpgKernelEntry *k = find_kernel(pl.kind, pl.op, pl.threads, pl.ept, pl.stages);
         if (!k) return SPAGHETTY_ERR_NOKERNEL;
         if (pl.smem_bytes > 48 * 1024) {
             if (cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -294,10 +299,86 @@ int call_r(const char *who, bool print, int rank, const double *u, double *s, co
     return rc;
 }
 
+// Tune file: one winner per line,
+//   gpu_name|sm_count|D0,D1,..|P0,P1,..|op_class|box0,box1,..|threads|ept|stages
+// (folded dims and 0-based folded permutation, as the autotuner writes them).
+int load_tune_file(const char *path, bool only_this_gpu) {
+    FILE *fh = std::fopen(path, "r");
+    if (!fh) return -1;
+    char name[256] = {0};
+    int sms = 0, have_dev = 0;
+    if (only_this_gpu) {
+        int dev = 0;
+        cudaDeviceProp prop;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaGetDeviceProperties(&prop, dev) == cudaSuccess) {
+            std::snprintf(name, sizeof(name), "%s", prop.name);
+            sms = prop.multiProcessorCount;
+            have_dev = 1;
+        } else {
+            cudaGetLastError();
+        }
+    }
+    int installed = 0;
+    char line[1024];
+    while (std::fgets(line, sizeof(line), fh)) {
+        if (line[0] == '#' || line[0] == '\n') continue;
+        char *fields[9];
+        int nf = 0;
+        char *save = nullptr;
+        for (char *tok = strtok_r(line, "|\n", &save); tok && nf < 9; tok = strtok_r(nullptr, "|\n", &save))
+            fields[nf++] = tok;
+        if (nf != 9) continue;
+        if (only_this_gpu && (!have_dev || std::strcmp(fields[0], name) != 0 || std::atoi(fields[1]) != sms))
+            continue;
+        int D[SPG_MAXR], P[SPG_MAXR], B[SPG_MAXR];
+        auto parse = [](char *txt, int *out) {
+            int n = 0;
+            char *sv = nullptr;
+            for (char *t = strtok_r(txt, ",", &sv); t && n < SPG_MAXR; t = strtok_r(nullptr, ",", &sv))
+                out[n++] = std::atoi(t);
+            return n;
+        };
+        const int r = parse(fields[2], D);
+        if (parse(fields[3], P) != r || parse(fields[5], B) != r || r < 2) continue;
+        for (int q = 0; q < r; ++q) P[q] += 1;   // the drop-in convention is 1-based
+        const int cls = std::atoi(fields[4]);
+        if (spaghetty_tune_set(r, D, P, cls, B, std::atoi(fields[6]), std::atoi(fields[7]),
+                               std::atoi(fields[8])) == SPAGHETTY_OK)
+            ++installed;
+    }
+    std::fclose(fh);
+    return installed;
+}
+
+void autoload_tune_file() {
+    static std::once_flag once;
+    std::call_once(once, [] {
+        const char *env = std::getenv("SPAGHETTY_GB300_TUNE_FILE");
+        if (env && !*env) return;             // explicitly disabled
+        std::string path;
+        if (env) {
+            path = env;
+        } else {
+            Dl_info info;
+            if (!dladdr((void *)&autoload_tune_file, &info) || !info.dli_fname) return;
+            path = info.dli_fname;
+            const size_t slash = path.rfind('/');
+            path = (slash == std::string::npos ? std::string(".") : path.substr(0, slash)) +
+                   "/tune_cache.txt";
+        }
+        load_tune_file(path.c_str(), true);
+    });
+}
+
 }  // namespace
 
 // ===========================================================================
 extern "C" {
+
+int spaghetty_tune_load(const char *path) {
+    if (!path) return -SPAGHETTY_ERR_NULL;
+    return load_tune_file(path, true);
+}
 
 const char *spaghetty_error_string(int code) {
     switch (code) {
@@ -369,6 +450,8 @@ int spaghetty_plan_query(int rank, const int *dims, const int *perm, int op,
     out->masked = pl.masked;
     out->grid = 0;
     out->vec = 0;
+    out->stages = pl.stages;
+    out->smem_bytes = pl.smem_bytes;
     return SPAGHETTY_OK;
 }
 
@@ -394,7 +477,11 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
         for (int d = R - 1; d >= 0; --d) { istr[d] = s; s *= fo.D[d]; }
     }
     std::vector<int64_t> got((size_t)n, -1);
-    const int64_t smem_elems = pl.smem_bytes / (int64_t)sizeof(double);
+    // one staging tile: the whole buffer of the register-staged kernel, one
+    // stage of the pipelined kernel
+    const int64_t smem_elems = pl.stages ? (int64_t)kp.stage
+                                         : pl.smem_bytes / (int64_t)sizeof(double);
+    if (pl.stages && (int64_t)pl.stages * kp.stage * 8 > pl.smem_bytes) return SPAGHETTY_ERR_CONFIG;
     std::vector<int64_t> sm((size_t)std::max<int64_t>(smem_elems, 1), -2);
     int64_t reads = 0, writes = 0;
     for (uint32_t t = 0; t < kp.ntiles; ++t) {
@@ -463,7 +550,7 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
 }
 
 int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const int *box,
-                       int threads, int ept) {
+                       int threads, int ept, int stages) {
     if (!box) {
         std::lock_guard<std::mutex> lk(g_mu);
         g_tune.clear();
@@ -475,9 +562,11 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     if (fo.empty || fo.rank < 2) return SPAGHETTY_ERR_CONFIG;
     if (threads != 128 && threads != 256 && threads != 512) return SPAGHETTY_ERR_CONFIG;
     if (ept != 1 && ept != 2 && ept != 4 && ept != 8) return SPAGHETTY_ERR_CONFIG;
+    if (stages != 0 && stages != 2 && stages != 3) return SPAGHETTY_ERR_CONFIG;
+    if (stages && ept < 2) return SPAGHETTY_ERR_CONFIG;
     const int opc = op == 0 ? OP_SCALE : (op == 1 ? OP_ACCF : OP_GEN);
     Plan pl;
-    rc = spg_plan(fo, opc, box, threads, ept, 152, &pl);
+    rc = spg_plan(fo, opc, box, threads, ept, stages, 152, &pl);
     if (rc) return rc;
     rc = spg_build_params(&pl, 0.5, 1.0);
     if (rc) return rc;
@@ -485,6 +574,7 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     for (int d = 0; d < SPG_MAXR; ++d) ov.box[d] = d < fo.rank ? box[d] : 1;
     ov.threads = threads;
     ov.ept = ept;
+    ov.stages = stages;
     std::lock_guard<std::mutex> lk(g_mu);
     g_tune[tune_key(fo, opc)] = ov;
     return SPAGHETTY_OK;

@@ -156,6 +156,108 @@ spg_tiled(const double *__restrict__ in, double *__restrict__ out,
 }
 
 // ---------------------------------------------------------------------------
+// Pipelined tiled kernel: the load phase issues 8-byte cp.async copies
+// straight from global memory into one of S shared-memory stages (masked
+// elements are zero-filled without touching memory), so S-1 boxes are in
+// flight per CTA while the current one is written out in output order.
+__device__ __forceinline__ void spg_cp_async8(uint32_t saddr, const double *src, uint32_t bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;\n" ::"r"(saddr), "l"(src),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void spg_cp_commit() {
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void spg_cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+template <int NT, int EPT, int OP, int S>
+__global__ void __launch_bounds__(NT)
+spg_tiled_async(const double *__restrict__ in, double *__restrict__ out,
+                const __grid_constant__ KParams p) {
+    extern __shared__ __align__(128) double sm[];
+    const uint32_t tid = threadIdx.x;
+    int32_t ioff[EPT], smw[EPT], ooff[EPT], smr[EPT];
+    uint32_t pkl[EPT], pks[EPT];
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+        const uint32_t e = tid + k * NT;
+        if (e < (uint32_t)p.vol) {
+            int32_t a, b, lin;
+            uint32_t pk;
+            spg_walk(p.ld, e, a, b, lin, pk);
+            ioff[k] = a;
+            smw[k] = (int32_t)e + (p.pad ? (int32_t)e / p.pad : 0);
+            pkl[k] = pk;
+            spg_walk(p.st, e, a, b, lin, pk);
+            ooff[k] = a;
+            smr[k] = lin + (p.pad ? lin / p.pad : 0);
+            pks[k] = pk;
+        } else {
+            ioff[k] = 0; smw[k] = 0; pkl[k] = SPG_INVALID;
+            ooff[k] = 0; smr[k] = 0; pks[k] = SPG_INVALID;
+        }
+    }
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
+    const uint32_t G = gridDim.x;
+    const uint32_t stage_bytes = (uint32_t)p.stage * 8u;
+
+    auto issue = [&](uint32_t t, int st) {
+        if (t < p.ntiles) {
+            int64_t ib, ob;
+            uint32_t limA, limB;
+            spg_box(p, t, ib, ob, limA, limB);
+            const double *src = in + ib;
+            const uint32_t sb = sbase + (uint32_t)st * stage_bytes;
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                if (pkl[k] != SPG_INVALID) {
+                    const bool v = spg_valid(pkl[k], limA, limB);
+                    spg_cp_async8(sb + (uint32_t)smw[k] * 8u, v ? src + ioff[k] : in, v ? 8u : 0u);
+                }
+            }
+        }
+        spg_cp_commit();
+    };
+
+    const double f = p.f, g = p.g;
+    uint32_t t = blockIdx.x;
+#pragma unroll
+    for (int q = 0; q < S - 1; ++q) issue(t + (uint32_t)q * G, q);
+    for (int it = 0; t < p.ntiles; t += G, ++it) {
+        const int st = it % S;
+        __syncthreads();                       // the stage refilled below is no longer read
+        issue(t + (uint32_t)(S - 1) * G, (it + S - 1) % S);
+        spg_cp_wait<S - 1>();                  // this thread's copies for box t have landed
+        __syncthreads();                       // ... and everyone else's
+        int64_t ib, ob;
+        uint32_t limA, limB;
+        spg_box(p, t, ib, ob, limA, limB);
+        double *dst = out + ob;
+        const double *tile = sm + st * p.stage;
+        double y[EPT];
+        if (spg_reads_out<OP>::value) {
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                y[k] = 0.0;
+                if (spg_valid(pks[k], limA, limB)) y[k] = spg_ld_out(dst + ooff[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            if (spg_valid(pks[k], limA, limB)) {
+                const double x = tile[smr[k]];
+                spg_st_out(dst + ooff[k],
+                           spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, f, g));
+            }
+        }
+    }
+    spg_cp_wait<0>();
+}
+
+// ---------------------------------------------------------------------------
 template <int NT, int EPT, int OP>
 __global__ void __launch_bounds__(NT)
 spg_direct(const double *__restrict__ in, double *__restrict__ out,
@@ -258,5 +360,6 @@ struct SpgKernelEntry {
     int op;         // SpgOp
     int threads;
     int ept;        // elements per thread (flat: vector width)
+    int stages;     // tiled: 0 = register-staged, 2/3 = cp.async pipeline depth
     const void *fn;
 };

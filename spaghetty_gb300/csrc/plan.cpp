@@ -143,6 +143,7 @@ int64_t largest_divisor_le(int64_t D, int64_t v) {
 
 static const int kTRun = 32;      // minimum contiguous doubles per box row
 static const int kVMax = 4096;    // largest box (512 threads x 8)
+static const int kDefaultStages = 3;
 
 static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L) {
     for (int d = 0; d < s.R; ++d) L[d] = 1;
@@ -243,7 +244,7 @@ static int64_t smem_wavefronts(const Plan &pl, int pad, const std::vector<int> &
 }
 
 int spg_plan(const Folded &fo, int op, const int *box_override, int threads_override,
-             int ept_override, int num_sms, Plan *pl) {
+             int ept_override, int stages_override, int num_sms, Plan *pl) {
     std::memset(pl, 0, sizeof(*pl));
     pl->fo = fo;
     pl->op = op;
@@ -285,10 +286,15 @@ int spg_plan(const Folded &fo, int op, const int *box_override, int threads_over
         pl->threads = threads_override;
         pl->ept = ept_override;
         if (pl->threads * pl->ept < vol) return SPAGHETTY_ERR_CONFIG;
+        pl->stages = stages_override;
     } else {
         int rc = pick_block((int)vol, &pl->threads, &pl->ept);
         if (rc) return rc;
+        pl->stages = kDefaultStages;
     }
+    if (pl->kind != KIND_TILED) pl->stages = 0;
+    if (pl->stages != 0 && pl->stages != 2 && pl->stages != 3) return SPAGHETTY_ERR_CONFIG;
+    if (pl->stages && pl->ept < 2) pl->stages = 0;
     return SPAGHETTY_OK;
 }
 
@@ -401,8 +407,11 @@ int spg_build_params(Plan *pl, double f, double g) {
             if (best < 0 || w < best) { best = w; kp.pad = c; }
         }
     }
-    pl->smem_bytes = pl->kind == KIND_TILED
-        ? (int)((kp.vol + (kp.pad ? kp.vol / kp.pad + 1 : 0)) * sizeof(double)) : 0;
+    const int tile = kp.vol + (kp.pad ? kp.vol / kp.pad + 1 : 0);
+    kp.stage = (tile + 15) & ~15;   // 128-byte aligned stages
+    if (pl->kind != KIND_TILED) pl->smem_bytes = 0;
+    else if (pl->stages) pl->smem_bytes = pl->stages * kp.stage * (int)sizeof(double);
+    else pl->smem_bytes = tile * (int)sizeof(double);
     return SPAGHETTY_OK;
 }
 

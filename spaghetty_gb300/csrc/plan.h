@@ -65,6 +65,7 @@ struct KParams {
     uint32_t ntiles;              // number of boxes
     int32_t vol;                  // elements per box
     int32_t pad;                  // shared-memory pad period (0 = none)
+    int32_t stage;                // staging-tile stride in elements (pipelined kernel)
     int32_t lenA, extA;           // partial dim A: box length and extent (or 1,1)
     int32_t lenB, extB;
     double f, g;
@@ -97,6 +98,7 @@ struct Plan {
     int op;
     int box[SPG_MAXR];
     int threads, ept;
+    int stages;               // tiled: 0 = register-staged, 2/3 = cp.async pipeline depth
     int run_in, run_out;
     int masked;
     int grid;                 // filled at launch time
@@ -108,6 +110,6 @@ struct Plan {
 int spg_fold(int rank, const int *dims, const int *perm, Folded *out);
 int spg_choose_op(double f, double g);
 int spg_plan(const Folded &fo, int op, const int *box_override, int threads_override,
-             int ept_override, int num_sms, Plan *out);
+             int ept_override, int stages_override, int num_sms, Plan *out);
 int spg_build_params(Plan *pl, double f, double g);
 int spg_selftest_host(void);

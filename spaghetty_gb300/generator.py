@@ -26,24 +26,32 @@ HEADER = """// GENERATED by spaghetty_gb300/generator.py -- do not edit.
 """
 
 
+STAGES = (2, 3)
+
+
 def variants(op: int):
+    """(kind, threads, ept, stages, function) for every compiled variant."""
     out = []
     for nt in THREADS:
         for ept in EPTS:
-            out.append(("KIND_TILED", nt, ept, "spg_tiled<%d, %d, %s>" % (nt, ept, OPS[op])))
+            out.append(("KIND_TILED", nt, ept, 0, "spg_tiled<%d, %d, %s>" % (nt, ept, OPS[op])))
+            if ept >= 2:
+                for st in STAGES:
+                    out.append(("KIND_TILED", nt, ept, st,
+                                "spg_tiled_async<%d, %d, %s, %d>" % (nt, ept, OPS[op], st)))
     for nt in THREADS:
         for ept in EPTS:
-            out.append(("KIND_DIRECT", nt, ept, "spg_direct<%d, %d, %s>" % (nt, ept, OPS[op])))
+            out.append(("KIND_DIRECT", nt, ept, 0, "spg_direct<%d, %d, %s>" % (nt, ept, OPS[op])))
     for vec in FLAT_VEC:
-        out.append(("KIND_FLAT", 256, vec, "spg_flat<%s, %d>" % (OPS[op], vec)))
+        out.append(("KIND_FLAT", 256, vec, 0, "spg_flat<%s, %d>" % (OPS[op], vec)))
     return out
 
 
 def emit_op(op: int) -> str:
     lines = [HEADER.format(opname=OPS[op])]
     lines.append("static const SpgKernelEntry kEntries[] = {")
-    for kind, nt, ept, fn in variants(op):
-        lines.append("    {%s, %s, %d, %d, (const void *)&%s}," % (kind, OPS[op], nt, ept, fn))
+    for kind, nt, ept, st, fn in variants(op):
+        lines.append("    {%s, %s, %d, %d, %d, (const void *)&%s}," % (kind, OPS[op], nt, ept, st, fn))
     lines.append("};")
     lines.append("const SpgKernelEntry *spg_kernels_op%d(int *n) {" % op)
     lines.append("    *n = (int)(sizeof(kEntries) / sizeof(kEntries[0]));")

@@ -143,7 +143,7 @@ def plan(dims: Sequence[int], perm: Sequence[int], op: int = 0):
         "box": [int(info.box[q]) for q in range(r)],
         "threads": info.threads, "ept": info.ept, "ntiles": int(info.ntiles),
         "run_in": info.run_in, "run_out": info.run_out, "pad": info.pad_period,
-        "masked": bool(info.masked),
+        "masked": bool(info.masked), "stages": info.stages, "smem_bytes": info.smem_bytes,
     }
 
 

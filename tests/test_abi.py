@@ -165,12 +165,12 @@ def test_tune_set_validation():
     L = lib()
     d = int_array((30, 30, 30, 30))
     p = int_array((4, 3, 2, 1))
-    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 30)), 128, 8) == 9  # too small
-    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 31)), 512, 8) == 9  # > extent
-    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 30)), 512, 8) == 0
+    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 30)), 128, 8, 3) == 9  # too small
+    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 31)), 512, 8, 3) == 9  # > extent
+    assert L.spaghetty_tune_set(4, d, p, 0, int_array((30, 2, 2, 30)), 512, 8, 0) == 0
     assert plan((30, 30, 30, 30), (4, 3, 2, 1))["box"] == [30, 2, 2, 30]
-    assert L.spaghetty_tune_set(4, d, p, 0, int_array((15, 1, 1, 15)), 256, 1) == 0
+    assert L.spaghetty_tune_set(4, d, p, 0, int_array((15, 1, 1, 15)), 256, 1, 0) == 0
     assert plan((30, 30, 30, 30), (4, 3, 2, 1))["box"] == [15, 1, 1, 15]
     assert verify((30, 30, 30, 30), (4, 3, 2, 1))[0] == 0
-    assert L.spaghetty_tune_set(0, None, None, 0, None, 0, 0) == 0   # clear
+    assert L.spaghetty_tune_set(0, None, None, 0, None, 0, 0, 0) == 0   # clear
     assert plan((30, 30, 30, 30), (4, 3, 2, 1))["box"] != [15, 1, 1, 15]
