@@ -253,6 +253,13 @@ def run_ours(args, ws, rank, local):
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(args.cpu_seconds)
 
+    batched = None
+    if not args.no_batched:
+        del bufs
+        torch.cuda.empty_cache()
+        batched = {"config": run_batched(args, dev),
+                   "small_tiles": run_batched(args, dev, ext4=(4, 12), ext6=(3, 6))}
+
     peak, peak_kind = peaks()
     roof = None
     if dom_n:
@@ -278,6 +285,7 @@ def run_ours(args, ws, rank, local):
         "roofline": roof,
         "e2e": e2e,
         "cpu_baseline": cpu,
+        "batched": batched,
         "clocks": clocks,
         "wall_s_timed_region": round(wall, 3),
     }
@@ -421,6 +429,65 @@ def run_reference(args, ws, rank):
     }
 
 
+def run_batched(args, dev, ext4=(8, 40), ext6=(6, 20), n=4096, seed=2024):
+    """The batched configuration: n uneven sorts (70% rank 4, extents
+    uniform in ext4; 30% rank 6, extents uniform in ext6; random perm, factor
+    uniform(-1,1), half sortacc) as ONE persistent launch replayed from a CUDA
+    graph, against one launch per sort.  Returns tiles/s and GB/s of both."""
+    import torch
+    from spaghetty_gb300.batched import Batch
+    from spaghetty_gb300.workloads import batched_mix
+    mix = batched_mix(n, seed=seed, ext4=ext4, ext6=ext6)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+    jobs = []
+    total_b = 0
+    for m in mix:
+        k = 1
+        for d in m["dims"]:
+            k *= d
+        u = torch.rand(k, dtype=torch.float64, device=dev, generator=gen) - 0.5
+        s = torch.rand(k, dtype=torch.float64, device=dev, generator=gen) - 0.5
+        jobs.append((u, s, m["dims"], m["perm"], m["factor"], 1.0 if m["acc"] else 0.0))
+        total_b += k * (24 if m["acc"] else 16)
+    b = Batch(jobs)
+    b.capture()
+    stream = torch.cuda.current_stream(dev)
+
+    def timed(fn, reps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps
+
+    for _ in range(args.warmup):
+        b.replay()
+        b.launch_plain()
+    torch.cuda.synchronize()
+    reps = max(1, args.steps)
+    t_graph = timed(b.replay, reps)
+    t_plain = timed(b.launch_plain, reps)
+    st = b.status()
+    info = b.info()
+    out = {"sorts": n, "ext4": list(ext4), "ext6": list(ext6), "status": st,
+           "work_units": info["units"], "bytes_per_launch": total_b,
+           "persistent_graph": {"tiles_per_s": round(n / t_graph, 1),
+                                "gbs": round(total_b / t_graph / 1e9, 1),
+                                "ms": round(t_graph * 1e3, 3), "launches": 1},
+           "one_launch_per_tile": {"tiles_per_s": round(n / t_plain, 1),
+                                   "gbs": round(total_b / t_plain / 1e9, 1),
+                                   "ms": round(t_plain * 1e3, 3), "launches": n},
+           "speedup": round(t_plain / t_graph, 3)}
+    b.close()
+    del jobs
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_case(args):
     """One sort case, W warm-up + K timed launches (the profiling workload)."""
     import torch
@@ -465,6 +532,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     ws, rank, local = dist_env()

@@ -230,6 +230,54 @@ int spaghetty_tune_load(const char *path);
  * invariant divisors).  Returns 0 when they pass.  Needs no GPU. */
 int spaghetty_selftest(void);
 
+/* ---- batched work lists (one persistent launch for many sorts) -------- */
+
+/* One sort of a batch.  Device pointers on the current device.  perm is
+ * 1-based; entries past `rank` are ignored.  acc_factor as in
+ * spaghetty_sort (0 = sort, 1 = sortacc). */
+typedef struct spaghetty_batch_entry {
+    const double *unsorted;
+    double *sorted;
+    int rank;
+    int dims[8];
+    int perm[8];
+    double factor;
+    double acc_factor;
+} spaghetty_batch_entry;
+
+typedef struct spaghetty_batch spaghetty_batch;
+
+/* Plan every entry, cut the work into units and upload the work list (the
+ * only allocation: job records, unit map, a counter and a status word).
+ * Rejects invalid entries (SPAGHETTY_ERR_* of the first bad one; its index
+ * from spaghetty_batch_bad_index()), host pointers, and any output that
+ * overlaps another buffer of the batch (inputs may be shared). */
+int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghetty_batch **out);
+int spaghetty_batch_bad_index(void);
+
+/* Enqueue the whole batch on `stream` as one counter reset plus ONE
+ * persistent kernel launch.  Capturable in a CUDA graph. */
+int spaghetty_batch_launch(spaghetty_batch *batch, void *stream);
+
+/* The same sorts as one launch each through spaghetty_sort_async (the plain
+ * path, for comparison). */
+int spaghetty_batch_launch_plain(spaghetty_batch *batch, void *stream);
+
+/* Synchronise `stream` and read (and clear) the device status word:
+ * SPAGHETTY_OK, or SPAGHETTY_ERR_DEVICE if a job record failed the kernel's
+ * validation and was skipped. */
+int spaghetty_batch_status(spaghetty_batch *batch, void *stream);
+
+/* {jobs, work units, algorithmic bytes per launch, shared bytes per CTA}. */
+int spaghetty_batch_info(const spaghetty_batch *batch, int64_t *info);
+
+/* Fault injection for tests, done by the host: overwrite job `index`'s kind
+ * in device memory with an invalid value.  The kernel must flag it in the
+ * status word and skip it without touching memory. */
+int spaghetty_batch_poison(spaghetty_batch *batch, int index);
+
+int spaghetty_batch_destroy(spaghetty_batch *batch);
+
 /* Library version string. */
 const char *spaghetty_version(void);
 

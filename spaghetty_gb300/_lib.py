@@ -41,6 +41,19 @@ class PlanInfo(ctypes.Structure):
     ]
 
 
+class BatchEntry(ctypes.Structure):
+    """Mirror of spaghetty_batch_entry."""
+    _fields_ = [
+        ("unsorted", ctypes.c_void_p),
+        ("sorted", ctypes.c_void_p),
+        ("rank", ctypes.c_int),
+        ("dims", ctypes.c_int * 8),
+        ("perm", ctypes.c_int * 8),
+        ("factor", ctypes.c_double),
+        ("acc_factor", ctypes.c_double),
+    ]
+
+
 # Every function the header declares, with its ctypes prototype.
 _R4 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 8 + [c_double_p]
 _R6 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 12 + [c_double_p]
@@ -72,6 +85,15 @@ PROTOTYPES = {
     "spaghetty_plan_verify": (ctypes.c_int, [ctypes.c_int, c_int_p, c_int_p, ctypes.c_int,
                                              ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     "spaghetty_tune_load": (ctypes.c_int, [ctypes.c_char_p]),
+    "spaghetty_batch_create": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_void_p)]),
+    "spaghetty_batch_bad_index": (ctypes.c_int, []),
+    "spaghetty_batch_launch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "spaghetty_batch_launch_plain": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "spaghetty_batch_status": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "spaghetty_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
+    "spaghetty_batch_poison": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "spaghetty_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "spaghetty_selftest": (ctypes.c_int, []),
     "spaghetty_version": (ctypes.c_char_p, []),
 }

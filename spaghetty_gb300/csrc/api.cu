@@ -25,6 +25,10 @@ const SpgKernelEntry *spg_kernels_op1(int *n);
 const SpgKernelEntry *spg_kernels_op2(int *n);
 const SpgKernelEntry *spg_kernels_op3(int *n);
 const SpgKernelEntry *spg_kernels_op4(int *n);
+const SpgKernelEntry *spg_kernels_op5(int *n);
+const SpgKernelEntry *spg_kernels_op6(int *n);
+const SpgKernelEntry *spg_kernels_op7(int *n);
+const SpgKernelEntry *spg_kernels_op8(int *n);
 
 namespace {
 
@@ -55,6 +59,10 @@ const SpgKernelEntry *find_kernel(int kind, int op, int nt, int ept, int stages)
         tabs[2] = spg_kernels_op2(&counts[2]);
         tabs[3] = spg_kernels_op3(&counts[3]);
         tabs[4] = spg_kernels_op4(&counts[4]);
+        tabs[5] = spg_kernels_op5(&counts[5]);
+        tabs[6] = spg_kernels_op6(&counts[6]);
+        tabs[7] = spg_kernels_op7(&counts[7]);
+        tabs[8] = spg_kernels_op8(&counts[8]);
     });
     if (op < 0 || op >= OP_COUNT) return nullptr;
     for (int i = 0; i < counts[op]; ++i) {
@@ -93,7 +101,7 @@ int occupancy(const SpgKernelEntry *k, int smem) {
 }
 
 std::string tune_key(const Folded &fo, int op) {
-    const int cls = (op == OP_COPY || op == OP_SCALE) ? 0 : (op == OP_GEN ? 2 : 1);
+    const int cls = spg_op_class(op);
     std::string k = std::to_string(fo.rank) + ":";
     for (int d = 0; d < fo.rank; ++d) k += std::to_string(fo.D[d]) + ",";
     k += ":";
@@ -136,8 +144,8 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
         int64_t n = pl.fo.nelem;
         int64_t work = (n / vec + 255) / 256;
         int grid = (int)std::min<int64_t>(std::max<int64_t>(work, 1), (int64_t)sms * 8);
-        double f = pl.kp.f, g = pl.kp.g;
-        void *args[] = {(void *)&u, (void *)&s, (void *)&n, (void *)&f, (void *)&g};
+        SpgFactor fac = pl.kp.fac;
+        void *args[] = {(void *)&u, (void *)&s, (void *)&n, (void *)&fac};
         pl.grid = grid;
         err = cudaLaunchKernel(k->fn, dim3(grid), dim3(256), args, 0, st);
     } else {
@@ -260,7 +268,7 @@ int sort_sync(int rank, const double *u, double *s, const int *dims, const int *
     }
     if (ks == 0) {
         if ((rc = grow(&sg.s, &sg.ns, n))) return rc;
-        if (pl.op != OP_COPY && pl.op != OP_SCALE)
+        if (spg_op_class(pl.op) != 0)
             if (cudaMemcpyAsync(sg.s, s, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) goto cuda_fail;
         ds_ptr = sg.s;
     }
@@ -564,7 +572,7 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     if (ept != 1 && ept != 2 && ept != 4 && ept != 8) return SPAGHETTY_ERR_CONFIG;
     if (stages != 0 && stages != 2 && stages != 3) return SPAGHETTY_ERR_CONFIG;
     if (stages && ept < 2) return SPAGHETTY_ERR_CONFIG;
-    const int opc = op == 0 ? OP_SCALE : (op == 1 ? OP_ACCF : OP_GEN);
+    const int opc = op == 0 ? OP_SORT_ANY : (op == 1 ? OP_ACC_ANY : OP_GEN);
     Plan pl;
     rc = spg_plan(fo, opc, box, threads, ept, stages, 152, &pl);
     if (rc) return rc;

@@ -1,0 +1,370 @@
+// batch.cu -- many independent sorts in ONE persistent kernel launch.
+//
+// A CCSD/CCSD(T) sweep issues thousands of uneven tce_sort_4/6 calls (the
+// triples code applies nine sortaccs to every t3 tile,
+// branches/spaghetty2/ccsd_t_tce_sort_list.txt).  One launch per call pays the
+// launch gap and a grid tail every time.  Here the host plans every sort once
+// (spg_plan_batch: one CTA shape for all), cuts each sort's boxes into work
+// units of ~16K elements, and uploads the job records plus a unit -> job map.
+// The persistent kernel's CTAs take units from an atomic counter; a CTA
+// rebuilds its per-element tables only when it moves to another sort.  The
+// launch (a counter reset and one kernel) is capturable in a CUDA graph.
+//
+// Faults are never raised on the device: a job record that fails validation
+// (kind, op, box volume, null pointers, unit range) sets a bit in a device
+// status word and is skipped; spaghetty_batch_status() reports it.  There is
+// no inter-CTA waiting of any kind.
+#include "../../include/spaghetty_gb300.h"
+#include "kernels.cuh"
+#include "plan.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#define SPG_BATCH_NT 256
+#define SPG_BATCH_EPT 8
+#define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
+#define SPG_BATCH_UNIT_ELEMS 16384
+
+struct BatchJob {
+    KParams kp;
+    const double *in;
+    double *out;
+    int32_t kind;
+    int32_t op;
+    uint32_t ubeg;     // first work unit of this job
+    uint32_t chunk;    // boxes per work unit
+};
+
+// Status word bits.
+#define SPG_ST_BAD_JOB 1
+#define SPG_ST_BAD_UNIT 2
+
+template <int OP>
+__device__ __forceinline__ void spg_batch_units(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
+                                                uint32_t b0, uint32_t b1, double *sm) {
+    if (j.kind == KIND_TILED) {
+        for (uint32_t t = b0; t < b1; ++t)
+            spg_tiled_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(j.kp, tb, j.in, j.out, t, sm);
+    } else {
+        for (uint32_t t = b0; t < b1; ++t)
+            spg_direct_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(j.kp, tb, j.in, j.out, t);
+    }
+}
+
+__global__ void __launch_bounds__(SPG_BATCH_NT)
+spg_batched(const BatchJob *__restrict__ jobs, uint32_t njobs,
+            const uint32_t *__restrict__ unit_job, uint32_t total_units,
+            uint32_t *counter, int *status, int smem_elems) {
+    extern __shared__ __align__(16) double sm[];
+    __shared__ BatchJob sj;
+    __shared__ uint32_t s_next;
+    __shared__ int s_ok;
+    const uint32_t tid = threadIdx.x;
+    SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> tb;
+    uint32_t cur = 0xFFFFFFFFu;
+    if (tid == 0) s_next = atomicAdd(counter, 1u);
+    __syncthreads();
+    for (;;) {
+        const uint32_t u = s_next;
+        if (u >= total_units) break;
+        const uint32_t j = unit_job[u];
+        __syncthreads();                      // everyone has read s_next
+        if (tid == 0) s_next = atomicAdd(counter, 1u);   // next unit, fetched early
+        if (j >= njobs) {
+            if (tid == 0) atomicOr(status, SPG_ST_BAD_UNIT);
+            __syncthreads();
+            continue;
+        }
+        if (j != cur) {
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(jobs + j);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&sj);
+            for (uint32_t i = tid; i < sizeof(BatchJob) / 4; i += SPG_BATCH_NT) dst[i] = src[i];
+            __syncthreads();
+            if (tid == 0) {
+                const KParams &p = sj.kp;
+                const int tile = p.vol + (p.pad > 0 ? p.vol / p.pad + 1 : 0);
+                bool ok = (sj.kind == KIND_TILED || sj.kind == KIND_DIRECT) && sj.op >= 0 &&
+                          sj.op < OP_COUNT && p.vol >= 1 && p.vol <= SPG_BATCH_VMAX &&
+                          p.pad >= 0 && sj.in != nullptr && sj.out != nullptr && sj.chunk >= 1 &&
+                          p.ntiles >= 1 && p.ld.n >= 0 && p.ld.n <= SPG_MAXR && p.st.n >= 0 &&
+                          p.st.n <= SPG_MAXR && p.grid.n >= 0 && p.grid.n <= SPG_MAXR &&
+                          (sj.kind != KIND_TILED || tile <= smem_elems) && u >= sj.ubeg;
+                s_ok = ok ? 1 : 0;
+                if (!ok) atomicOr(status, SPG_ST_BAD_JOB);
+            }
+            __syncthreads();
+            if (s_ok) {
+                if (sj.kind == KIND_TILED) tb.build_tiled(sj.kp, tid);
+                else tb.build_direct(sj.kp, tid);
+            }
+            cur = j;
+        }
+        if (s_ok) {
+            const uint32_t b0 = (u - sj.ubeg) * sj.chunk;
+            const uint32_t b1 = min(b0 + sj.chunk, sj.kp.ntiles);
+            switch (sj.op) {
+                case OP_SORT_ONE: spg_batch_units<OP_SORT_ONE>(sj, tb, b0, b1, sm); break;
+                case OP_SORT_NEG: spg_batch_units<OP_SORT_NEG>(sj, tb, b0, b1, sm); break;
+                case OP_SORT_POW2: spg_batch_units<OP_SORT_POW2>(sj, tb, b0, b1, sm); break;
+                case OP_SORT_ANY: spg_batch_units<OP_SORT_ANY>(sj, tb, b0, b1, sm); break;
+                case OP_ACC_ONE: spg_batch_units<OP_ACC_ONE>(sj, tb, b0, b1, sm); break;
+                case OP_ACC_NEG: spg_batch_units<OP_ACC_NEG>(sj, tb, b0, b1, sm); break;
+                case OP_ACC_POW2: spg_batch_units<OP_ACC_POW2>(sj, tb, b0, b1, sm); break;
+                case OP_ACC_ANY: spg_batch_units<OP_ACC_ANY>(sj, tb, b0, b1, sm); break;
+                default: spg_batch_units<OP_GEN>(sj, tb, b0, b1, sm); break;
+            }
+        }
+        __syncthreads();                      // unit done: sj and the tile may be replaced
+    }
+}
+
+// ===========================================================================
+struct spaghetty_batch {
+    int dev = 0;
+    int n = 0;
+    uint32_t njobs = 0;
+    uint32_t total_units = 0;
+    int smem_elems = 0;
+    BatchJob *d_jobs = nullptr;
+    uint32_t *d_unit_job = nullptr;
+    uint32_t *d_words = nullptr;      // [0] = unit counter, [1] = status word
+    std::vector<spaghetty_batch_entry> entries;
+    std::vector<BatchJob> jobs;       // host copy of the job records
+    int64_t bytes = 0;                // algorithmic bytes of one launch
+};
+
+namespace {
+thread_local int g_batch_bad_index = -1;
+
+bool is_device_ptr(const void *p, int *dev) {
+    cudaPointerAttributes at;
+    std::memset(&at, 0, sizeof(at));
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
+        *dev = at.device;
+        return true;
+    }
+    return false;
+}
+
+int grid_for(spaghetty_batch *b) {
+    int sms = 0, nb = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev) != cudaSuccess) sms = 152;
+    const size_t smem = (size_t)b->smem_elems * sizeof(double);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_batched, SPG_BATCH_NT, smem) != cudaSuccess ||
+        nb < 1)
+        nb = 1;
+    cudaGetLastError();
+    int64_t g = (int64_t)sms * nb;
+    g = std::min<int64_t>(g, std::max<uint32_t>(b->total_units, 1));
+    return (int)g;
+}
+}  // namespace
+
+extern "C" {
+
+int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghetty_batch **out) {
+    g_batch_bad_index = -1;
+    if (!out) return SPAGHETTY_ERR_NULL;
+    *out = nullptr;
+    if (n < 0 || (n > 0 && !entries)) return SPAGHETTY_ERR_NULL;
+    spaghetty_batch *b = new spaghetty_batch();
+    b->n = n;
+    b->entries.assign(entries, entries + n);
+    if (cudaGetDevice(&b->dev) != cudaSuccess) {
+        cudaGetLastError();
+        delete b;
+        return SPAGHETTY_ERR_CUDA;
+    }
+    std::vector<uint32_t> unit_job;
+    struct Range { uintptr_t lo, hi; int idx; bool out; };
+    std::vector<Range> ranges;
+    int rc = SPAGHETTY_OK;
+    for (int i = 0; i < n && rc == SPAGHETTY_OK; ++i) {
+        const spaghetty_batch_entry &e = entries[i];
+        Folded fo;
+        rc = spg_fold(e.rank, e.dims, e.perm, &fo);
+        if (rc) { g_batch_bad_index = i; break; }
+        if (fo.empty) continue;
+        if (!e.unsorted || !e.sorted) { rc = SPAGHETTY_ERR_NULL; g_batch_bad_index = i; break; }
+        int du = -1, ds = -1;
+        if (!is_device_ptr(e.unsorted, &du) || !is_device_ptr(e.sorted, &ds) || du != b->dev ||
+            ds != b->dev) {
+            rc = SPAGHETTY_ERR_MEMSPACE;
+            g_batch_bad_index = i;
+            break;
+        }
+        const uintptr_t nb = (uintptr_t)fo.nelem * sizeof(double);
+        ranges.push_back({(uintptr_t)e.unsorted, (uintptr_t)e.unsorted + nb, i, false});
+        ranges.push_back({(uintptr_t)e.sorted, (uintptr_t)e.sorted + nb, i, true});
+        Plan pl;
+        const int op = spg_choose_op(e.factor, e.acc_factor);
+        rc = spg_plan_batch(fo, op, &pl);
+        if (!rc) rc = spg_build_params(&pl, e.factor, e.acc_factor);
+        if (rc) { g_batch_bad_index = i; break; }
+        BatchJob j;
+        std::memset(&j, 0, sizeof(j));
+        j.kp = pl.kp;
+        j.in = e.unsorted;
+        j.out = e.sorted;
+        j.kind = pl.kind;
+        j.op = op;
+        j.chunk = (uint32_t)std::max(1, SPG_BATCH_UNIT_ELEMS / std::max(1, (int)pl.kp.vol));
+        j.ubeg = (uint32_t)unit_job.size();
+        const uint32_t units = (pl.kp.ntiles + j.chunk - 1) / j.chunk;
+        if ((uint64_t)unit_job.size() + units > 0xFFFFFFF0ull) { rc = SPAGHETTY_ERR_OVERFLOW; break; }
+        for (uint32_t q = 0; q < units; ++q) unit_job.push_back((uint32_t)b->jobs.size());
+        if (pl.kind == KIND_TILED)
+            b->smem_elems = std::max(b->smem_elems, pl.kp.vol + (pl.kp.pad ? pl.kp.vol / pl.kp.pad + 1 : 0));
+        b->bytes += fo.nelem * (spg_op_class(op) == 0 ? 16 : 24);
+        b->jobs.push_back(j);
+    }
+    if (rc == SPAGHETTY_OK) {
+        // No output may overlap any other buffer of the batch (inputs may be
+        // shared between sorts): outputs pairwise disjoint, then every input
+        // checked against the sorted outputs.
+        std::vector<Range> outs, ins;
+        for (const Range &r : ranges) (r.out ? outs : ins).push_back(r);
+        std::sort(outs.begin(), outs.end(), [](const Range &a, const Range &c) { return a.lo < c.lo; });
+        for (size_t q = 1; q < outs.size() && rc == SPAGHETTY_OK; ++q)
+            if (outs[q].lo < outs[q - 1].hi) { rc = SPAGHETTY_ERR_ALIAS; g_batch_bad_index = outs[q].idx; }
+        for (size_t q = 0; q < ins.size() && rc == SPAGHETTY_OK; ++q) {
+            // first output whose end lies beyond this input's start
+            auto it = std::upper_bound(outs.begin(), outs.end(), ins[q].lo,
+                                       [](uintptr_t v, const Range &r) { return v < r.hi; });
+            if (it != outs.end() && it->lo < ins[q].hi) { rc = SPAGHETTY_ERR_ALIAS; g_batch_bad_index = ins[q].idx; }
+        }
+    }
+    if (rc != SPAGHETTY_OK) {
+        delete b;
+        return rc;
+    }
+    b->njobs = (uint32_t)b->jobs.size();
+    b->total_units = (uint32_t)unit_job.size();
+    b->smem_elems = std::max(b->smem_elems, 2);
+    bool ok = cudaMalloc((void **)&b->d_words, 2 * sizeof(uint32_t)) == cudaSuccess &&
+              cudaMemset(b->d_words, 0, 2 * sizeof(uint32_t)) == cudaSuccess;
+    if (ok && b->njobs) {
+        ok = cudaMalloc((void **)&b->d_jobs, b->jobs.size() * sizeof(BatchJob)) == cudaSuccess &&
+             cudaMalloc((void **)&b->d_unit_job, unit_job.size() * sizeof(uint32_t)) == cudaSuccess &&
+             cudaMemcpy(b->d_jobs, b->jobs.data(), b->jobs.size() * sizeof(BatchJob),
+                        cudaMemcpyHostToDevice) == cudaSuccess &&
+             cudaMemcpy(b->d_unit_job, unit_job.data(), unit_job.size() * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    if (!ok) {
+        cudaGetLastError();
+        spaghetty_batch_destroy(b);
+        return SPAGHETTY_ERR_CUDA;
+    }
+    if ((size_t)b->smem_elems * sizeof(double) > 48 * 1024) {
+        if (cudaFuncSetAttribute(spg_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 b->smem_elems * (int)sizeof(double)) != cudaSuccess) {
+            cudaGetLastError();
+            spaghetty_batch_destroy(b);
+            return SPAGHETTY_ERR_CUDA;
+        }
+    }
+    *out = b;
+    return SPAGHETTY_OK;
+}
+
+int spaghetty_batch_bad_index(void) { return g_batch_bad_index; }
+
+int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
+    if (!b) return SPAGHETTY_ERR_NULL;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (b->total_units == 0) return SPAGHETTY_OK;
+    if (cudaMemsetAsync(b->d_words, 0, sizeof(uint32_t), st) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    const int grid = grid_for(b);
+    uint32_t *counter = b->d_words;
+    int *status = (int *)(b->d_words + 1);
+    const BatchJob *jobs = b->d_jobs;
+    const uint32_t *uj = b->d_unit_job;
+    uint32_t nj = b->njobs, tu = b->total_units;
+    int se = b->smem_elems;
+    void *args[] = {(void *)&jobs, (void *)&nj, (void *)&uj, (void *)&tu,
+                    (void *)&counter, (void *)&status, (void *)&se};
+    if (cudaLaunchKernel((const void *)spg_batched, dim3(grid), dim3(SPG_BATCH_NT), args,
+                         (size_t)b->smem_elems * sizeof(double), st) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    return SPAGHETTY_OK;
+}
+
+int spaghetty_batch_launch_plain(spaghetty_batch *b, void *stream) {
+    if (!b) return SPAGHETTY_ERR_NULL;
+    for (const spaghetty_batch_entry &e : b->entries) {
+        int rc = spaghetty_sort_async(e.rank, e.unsorted, e.sorted, e.dims, e.perm, e.factor,
+                                      e.acc_factor, stream);
+        if (rc) return rc;
+    }
+    return SPAGHETTY_OK;
+}
+
+int spaghetty_batch_status(spaghetty_batch *b, void *stream) {
+    if (!b) return SPAGHETTY_ERR_NULL;
+    if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    int st = 0;
+    if (cudaMemcpy(&st, b->d_words + 1, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    if (cudaMemset(b->d_words + 1, 0, sizeof(int)) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    return st ? SPAGHETTY_ERR_DEVICE : SPAGHETTY_OK;
+}
+
+int spaghetty_batch_info(const spaghetty_batch *b, int64_t *info) {
+    if (!b || !info) return SPAGHETTY_ERR_NULL;
+    info[0] = b->njobs;
+    info[1] = b->total_units;
+    info[2] = b->bytes;
+    info[3] = b->smem_elems * (int64_t)sizeof(double);
+    return SPAGHETTY_OK;
+}
+
+int spaghetty_batch_poison(spaghetty_batch *b, int index) {
+    // Host-side fault injection for tests: overwrite one job record's kind
+    // with an invalid value in device memory (the kernel must flag and skip
+    // it without touching memory).
+    if (!b) return SPAGHETTY_ERR_NULL;
+    if (index < 0 || (uint32_t)index >= b->njobs) return SPAGHETTY_ERR_BATCH;
+    BatchJob j = b->jobs[index];
+    j.kind = 99;
+    if (cudaMemcpy(b->d_jobs + index, &j, sizeof(BatchJob), cudaMemcpyHostToDevice) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    return SPAGHETTY_OK;
+}
+
+int spaghetty_batch_destroy(spaghetty_batch *b) {
+    if (!b) return SPAGHETTY_OK;
+    if (b->d_jobs) cudaFree(b->d_jobs);
+    if (b->d_unit_job) cudaFree(b->d_unit_job);
+    if (b->d_words) cudaFree(b->d_words);
+    cudaGetLastError();
+    delete b;
+    return SPAGHETTY_OK;
+}
+
+}  // extern "C"

@@ -21,22 +21,49 @@
 #include <stdint.h>
 #include "plan.h"
 
-template <int OP>
-__device__ __forceinline__ double spg_apply(double x, double y, double f, double g) {
-    if (OP == OP_COPY) return x;
-    if (OP == OP_SCALE) return __dmul_rn(x, f);
-    if (OP == OP_ACC1) return __dadd_rn(y, x);
-    if (OP == OP_ACCF) return __dadd_rn(y, __dmul_rn(x, f));
-    return __dadd_rn(__dmul_rn(g, y), __dmul_rn(f, x));   // OP_GEN
+// x * f for f = +-2^k: when x is normal and x*f is normal, the product is
+// exact and equals x with k added to its exponent field and f's sign applied
+// -- integer operations only.  Every other input (zero, subnormal, inf,
+// NaN) or result (overflow, underflow) takes the rounded multiply, so the
+// bits always equal __dmul_rn(x, f).
+__device__ __forceinline__ double spg_pow2(double x, const SpgFactor &F) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    if (e - 1u < 2046u && (uint32_t)((int32_t)e + F.k) - 1u < 2046u)
+        return __longlong_as_double((long long)((b + (uint64_t)F.kshift) ^ F.sgn));
+    return __dmul_rn(x, F.f);
+}
+
+// x * -1: the sign bit flipped (exact for every non-NaN x, inf included);
+// NaN takes the multiply.
+__device__ __forceinline__ double spg_neg(double x, const SpgFactor &F) {
+    const uint64_t b = (uint64_t)__double_as_longlong(x);
+    if ((b & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull)
+        return __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
+    return __dmul_rn(x, F.f);
 }
 
 template <int OP>
-struct spg_reads_out { static constexpr bool value = (OP == OP_ACC1 || OP == OP_ACCF || OP == OP_GEN); };
+__device__ __forceinline__ double spg_apply(double x, double y, const SpgFactor &F) {
+    if (OP == OP_SORT_ONE) return x;
+    if (OP == OP_SORT_NEG) return spg_neg(x, F);
+    if (OP == OP_SORT_POW2) return spg_pow2(x, F);
+    if (OP == OP_SORT_ANY) return __dmul_rn(x, F.f);
+    if (OP == OP_ACC_ONE) return __dadd_rn(y, x);
+    if (OP == OP_ACC_NEG) return __dadd_rn(y, spg_neg(x, F));
+    if (OP == OP_ACC_POW2) return __dadd_rn(y, spg_pow2(x, F));
+    if (OP == OP_ACC_ANY) return __dadd_rn(y, __dmul_rn(x, F.f));
+    return __dadd_rn(__dmul_rn(F.g, y), __dmul_rn(F.f, x));   // OP_GEN
+}
 
-// Input is read exactly once: keep it out of L1 and mark it evict-first.
-__device__ __forceinline__ double spg_ld_in(const double *p) { return __ldcs(p); }
-__device__ __forceinline__ double spg_ld_out(const double *p) { return __ldcs(p); }
-__device__ __forceinline__ void spg_st_out(double *p, double v) { __stcs(p, v); }
+template <int OP>
+struct spg_reads_out { static constexpr bool value = (OP >= OP_ACC_ONE); };
+
+// Input is read once (read-only path); outputs use the default write-back
+// policy so that L2 merges the partial sectors two neighbouring boxes write.
+__device__ __forceinline__ double spg_ld_in(const double *p) { return __ldg(p); }
+__device__ __forceinline__ double spg_ld_out(const double *p) { return *p; }
+__device__ __forceinline__ void spg_st_out(double *p, double v) { *p = v; }
 
 // Decompose a box-local element index along a walk.  Host-callable too, so
 // that spaghetty_plan_verify can replay the exact index arithmetic on the CPU.
@@ -92,67 +119,132 @@ __host__ __device__ __forceinline__ bool spg_valid(uint32_t pk, uint32_t limA, u
 #define SPG_INVALID 0xFFFFFFFFu
 
 // ---------------------------------------------------------------------------
+// Per-thread element tables of one box shape, built once per CTA (and again
+// by the batched kernel whenever it switches to another sort).
+//   tiled:  ioff/smw/pkl = load side (input offset, shared slot, mask coords)
+//           ooff/smr/pks = store side (output offset, shared slot, mask coords)
+//   direct: ioff/ooff/pkl only (input and output offset of the same element)
+template <int NT, int EPT>
+struct SpgTab {
+    int32_t ioff[EPT], smw[EPT], ooff[EPT], smr[EPT];
+    uint32_t pkl[EPT], pks[EPT];
+
+    __device__ __forceinline__ void build_tiled(const KParams &p, uint32_t tid) {
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            const uint32_t e = tid + k * NT;
+            if (e < (uint32_t)p.vol) {
+                int32_t a, b, lin;
+                uint32_t pk;
+                spg_walk(p.ld, e, a, b, lin, pk);
+                ioff[k] = a;
+                smw[k] = (int32_t)e + (p.pad ? (int32_t)e / p.pad : 0);
+                pkl[k] = pk;
+                spg_walk(p.st, e, a, b, lin, pk);
+                ooff[k] = a;
+                smr[k] = lin + (p.pad ? lin / p.pad : 0);
+                pks[k] = pk;
+            } else {
+                ioff[k] = 0; smw[k] = 0; pkl[k] = SPG_INVALID;
+                ooff[k] = 0; smr[k] = 0; pks[k] = SPG_INVALID;
+            }
+        }
+    }
+
+    __device__ __forceinline__ void build_direct(const KParams &p, uint32_t tid) {
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            const uint32_t e = tid + k * NT;
+            if (e < (uint32_t)p.vol) {
+                int32_t a, b, lin;
+                uint32_t pk;
+                spg_walk(p.ld, e, a, b, lin, pk);
+                ioff[k] = a; ooff[k] = b; pkl[k] = pk;
+            } else {
+                ioff[k] = 0; ooff[k] = 0; pkl[k] = SPG_INVALID;
+            }
+            smw[k] = 0; smr[k] = 0; pks[k] = SPG_INVALID;
+        }
+    }
+};
+
+// One box of the register-staged tiled kernel.  Contains two CTA barriers:
+// every thread of the CTA must call it for the same box.
+template <int NT, int EPT, int OP>
+__device__ __forceinline__ void spg_tiled_box(const KParams &p, const SpgTab<NT, EPT> &tb,
+                                              const double *__restrict__ in,
+                                              double *__restrict__ out, uint32_t t, double *sm) {
+    int64_t ib, ob;
+    uint32_t limA, limB;
+    spg_box(p, t, ib, ob, limA, limB);
+    const double *src = in + ib;
+    double *dst = out + ob;
+    const SpgFactor fac = p.fac;
+    double v[EPT];
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+        v[k] = 0.0;
+        if (spg_valid(tb.pkl[k], limA, limB)) v[k] = spg_ld_in(src + tb.ioff[k]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < EPT; ++k)
+        if (tb.pkl[k] != SPG_INVALID) sm[tb.smw[k]] = v[k];
+    __syncthreads();
+    double y[EPT];
+    if (spg_reads_out<OP>::value) {
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            y[k] = 0.0;
+            if (spg_valid(tb.pks[k], limA, limB)) y[k] = spg_ld_out(dst + tb.ooff[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+        if (spg_valid(tb.pks[k], limA, limB)) {
+            const double x = sm[tb.smr[k]];
+            spg_st_out(dst + tb.ooff[k],
+                       spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, fac));
+        }
+    }
+}
+
+// One box of the direct kernel (no barrier).
+template <int NT, int EPT, int OP>
+__device__ __forceinline__ void spg_direct_box(const KParams &p, const SpgTab<NT, EPT> &tb,
+                                               const double *__restrict__ in,
+                                               double *__restrict__ out, uint32_t t) {
+    int64_t ib, ob;
+    uint32_t limA, limB;
+    spg_box(p, t, ib, ob, limA, limB);
+    const double *src = in + ib;
+    double *dst = out + ob;
+    const SpgFactor fac = p.fac;
+    double v[EPT], y[EPT];
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+        v[k] = 0.0; y[k] = 0.0;
+        if (spg_valid(tb.pkl[k], limA, limB)) {
+            v[k] = spg_ld_in(src + tb.ioff[k]);
+            if (spg_reads_out<OP>::value) y[k] = spg_ld_out(dst + tb.ooff[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < EPT; ++k)
+        if (spg_valid(tb.pkl[k], limA, limB))
+            spg_st_out(dst + tb.ooff[k], spg_apply<OP>(v[k], y[k], fac));
+}
+
+// ---------------------------------------------------------------------------
 template <int NT, int EPT, int OP>
 __global__ void __launch_bounds__(NT)
 spg_tiled(const double *__restrict__ in, double *__restrict__ out,
           const __grid_constant__ KParams p) {
     extern __shared__ double sm[];
-    const uint32_t tid = threadIdx.x;
-    int32_t ioff[EPT], smw[EPT], ooff[EPT], smr[EPT];
-    uint32_t pkl[EPT], pks[EPT];
-#pragma unroll
-    for (int k = 0; k < EPT; ++k) {
-        const uint32_t e = tid + k * NT;
-        if (e < (uint32_t)p.vol) {
-            int32_t a, b, lin;
-            uint32_t pk;
-            spg_walk(p.ld, e, a, b, lin, pk);
-            ioff[k] = a;
-            smw[k] = (int32_t)e + (p.pad ? (int32_t)e / p.pad : 0);
-            pkl[k] = pk;
-            spg_walk(p.st, e, a, b, lin, pk);
-            ooff[k] = a;
-            smr[k] = lin + (p.pad ? lin / p.pad : 0);
-            pks[k] = pk;
-        } else {
-            ioff[k] = 0; smw[k] = 0; pkl[k] = SPG_INVALID;
-            ooff[k] = 0; smr[k] = 0; pks[k] = SPG_INVALID;
-        }
-    }
-    const double f = p.f, g = p.g;
-    for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-        int64_t ib, ob;
-        uint32_t limA, limB;
-        spg_box(p, t, ib, ob, limA, limB);
-        const double *src = in + ib;
-        double *dst = out + ob;
-        double v[EPT];
-#pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            v[k] = 0.0;
-            if (spg_valid(pkl[k], limA, limB)) v[k] = spg_ld_in(src + ioff[k]);
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < EPT; ++k)
-            if (pkl[k] != SPG_INVALID) sm[smw[k]] = v[k];
-        __syncthreads();
-        double y[EPT];
-        if (spg_reads_out<OP>::value) {
-#pragma unroll
-            for (int k = 0; k < EPT; ++k) {
-                y[k] = 0.0;
-                if (spg_valid(pks[k], limA, limB)) y[k] = spg_ld_out(dst + ooff[k]);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            if (spg_valid(pks[k], limA, limB)) {
-                const double x = sm[smr[k]];
-                spg_st_out(dst + ooff[k], spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, f, g));
-            }
-        }
-    }
+    SpgTab<NT, EPT> tb;
+    tb.build_tiled(p, threadIdx.x);
+    for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x)
+        spg_tiled_box<NT, EPT, OP>(p, tb, in, out, t, sm);
 }
 
 // ---------------------------------------------------------------------------
@@ -178,28 +270,8 @@ __global__ void __launch_bounds__(NT)
 spg_tiled_async(const double *__restrict__ in, double *__restrict__ out,
                 const __grid_constant__ KParams p) {
     extern __shared__ __align__(128) double sm[];
-    const uint32_t tid = threadIdx.x;
-    int32_t ioff[EPT], smw[EPT], ooff[EPT], smr[EPT];
-    uint32_t pkl[EPT], pks[EPT];
-#pragma unroll
-    for (int k = 0; k < EPT; ++k) {
-        const uint32_t e = tid + k * NT;
-        if (e < (uint32_t)p.vol) {
-            int32_t a, b, lin;
-            uint32_t pk;
-            spg_walk(p.ld, e, a, b, lin, pk);
-            ioff[k] = a;
-            smw[k] = (int32_t)e + (p.pad ? (int32_t)e / p.pad : 0);
-            pkl[k] = pk;
-            spg_walk(p.st, e, a, b, lin, pk);
-            ooff[k] = a;
-            smr[k] = lin + (p.pad ? lin / p.pad : 0);
-            pks[k] = pk;
-        } else {
-            ioff[k] = 0; smw[k] = 0; pkl[k] = SPG_INVALID;
-            ooff[k] = 0; smr[k] = 0; pks[k] = SPG_INVALID;
-        }
-    }
+    SpgTab<NT, EPT> tb;
+    tb.build_tiled(p, threadIdx.x);
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
     const uint32_t G = gridDim.x;
     const uint32_t stage_bytes = (uint32_t)p.stage * 8u;
@@ -213,16 +285,17 @@ spg_tiled_async(const double *__restrict__ in, double *__restrict__ out,
             const uint32_t sb = sbase + (uint32_t)st * stage_bytes;
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
-                if (pkl[k] != SPG_INVALID) {
-                    const bool v = spg_valid(pkl[k], limA, limB);
-                    spg_cp_async8(sb + (uint32_t)smw[k] * 8u, v ? src + ioff[k] : in, v ? 8u : 0u);
+                if (tb.pkl[k] != SPG_INVALID) {
+                    const bool v = spg_valid(tb.pkl[k], limA, limB);
+                    spg_cp_async8(sb + (uint32_t)tb.smw[k] * 8u, v ? src + tb.ioff[k] : in,
+                                  v ? 8u : 0u);
                 }
             }
         }
         spg_cp_commit();
     };
 
-    const double f = p.f, g = p.g;
+    const SpgFactor fac = p.fac;
     uint32_t t = blockIdx.x;
 #pragma unroll
     for (int q = 0; q < S - 1; ++q) issue(t + (uint32_t)q * G, q);
@@ -242,15 +315,15 @@ spg_tiled_async(const double *__restrict__ in, double *__restrict__ out,
 #pragma unroll
             for (int k = 0; k < EPT; ++k) {
                 y[k] = 0.0;
-                if (spg_valid(pks[k], limA, limB)) y[k] = spg_ld_out(dst + ooff[k]);
+                if (spg_valid(tb.pks[k], limA, limB)) y[k] = spg_ld_out(dst + tb.ooff[k]);
             }
         }
 #pragma unroll
         for (int k = 0; k < EPT; ++k) {
-            if (spg_valid(pks[k], limA, limB)) {
-                const double x = tile[smr[k]];
-                spg_st_out(dst + ooff[k],
-                           spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, f, g));
+            if (spg_valid(tb.pks[k], limA, limB)) {
+                const double x = tile[tb.smr[k]];
+                spg_st_out(dst + tb.ooff[k],
+                           spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, fac));
             }
         }
     }
@@ -262,42 +335,10 @@ template <int NT, int EPT, int OP>
 __global__ void __launch_bounds__(NT)
 spg_direct(const double *__restrict__ in, double *__restrict__ out,
            const __grid_constant__ KParams p) {
-    const uint32_t tid = threadIdx.x;
-    int32_t ioff[EPT], ooff[EPT];
-    uint32_t pkk[EPT];
-#pragma unroll
-    for (int k = 0; k < EPT; ++k) {
-        const uint32_t e = tid + k * NT;
-        if (e < (uint32_t)p.vol) {
-            int32_t a, b, lin;
-            uint32_t pk;
-            spg_walk(p.ld, e, a, b, lin, pk);
-            ioff[k] = a; ooff[k] = b; pkk[k] = pk;
-        } else {
-            ioff[k] = 0; ooff[k] = 0; pkk[k] = SPG_INVALID;
-        }
-    }
-    const double f = p.f, g = p.g;
-    for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
-        int64_t ib, ob;
-        uint32_t limA, limB;
-        spg_box(p, t, ib, ob, limA, limB);
-        const double *src = in + ib;
-        double *dst = out + ob;
-        double v[EPT], y[EPT];
-#pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            v[k] = 0.0; y[k] = 0.0;
-            if (spg_valid(pkk[k], limA, limB)) {
-                v[k] = spg_ld_in(src + ioff[k]);
-                if (spg_reads_out<OP>::value) y[k] = spg_ld_out(dst + ooff[k]);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < EPT; ++k)
-            if (spg_valid(pkk[k], limA, limB))
-                spg_st_out(dst + ooff[k], spg_apply<OP>(v[k], y[k], f, g));
-    }
+    SpgTab<NT, EPT> tb;
+    tb.build_direct(p, threadIdx.x);
+    for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x)
+        spg_direct_box<NT, EPT, OP>(p, tb, in, out, t);
 }
 
 // ---------------------------------------------------------------------------
@@ -306,8 +347,8 @@ spg_direct(const double *__restrict__ in, double *__restrict__ out,
 // by thread 0 of block 0.
 template <int OP, int VEC>
 __global__ void __launch_bounds__(256)
-spg_flat(const double *__restrict__ in, double *__restrict__ out, int64_t n, double f,
-         double g) {
+spg_flat(const double *__restrict__ in, double *__restrict__ out, int64_t n,
+         const SpgFactor fac) {
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (VEC == 2) {
@@ -326,8 +367,8 @@ spg_flat(const double *__restrict__ in, double *__restrict__ out, int64_t n, dou
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 double2 r;
-                r.x = spg_apply<OP>(x[u].x, y[u].x, f, g);
-                r.y = spg_apply<OP>(x[u].y, y[u].y, f, g);
+                r.x = spg_apply<OP>(x[u].x, y[u].x, fac);
+                r.y = spg_apply<OP>(x[u].y, y[u].y, fac);
                 __stcs(out2 + j + u * stride, r);
             }
         }
@@ -336,20 +377,20 @@ spg_flat(const double *__restrict__ in, double *__restrict__ out, int64_t n, dou
             double2 y = make_double2(0.0, 0.0);
             if (spg_reads_out<OP>::value) y = __ldcs(out2 + j);
             double2 r;
-            r.x = spg_apply<OP>(x.x, y.x, f, g);
-            r.y = spg_apply<OP>(x.y, y.y, f, g);
+            r.x = spg_apply<OP>(x.x, y.x, fac);
+            r.y = spg_apply<OP>(x.y, y.y, fac);
             __stcs(out2 + j, r);
         }
         if ((n & 1) && i0 == 0) {
             const double x = in[n - 1];
             const double y = spg_reads_out<OP>::value ? out[n - 1] : 0.0;
-            out[n - 1] = spg_apply<OP>(x, y, f, g);
+            out[n - 1] = spg_apply<OP>(x, y, fac);
         }
     } else {
         for (int64_t j = i0; j < n; j += stride) {
             const double x = __ldcs(in + j);
             const double y = spg_reads_out<OP>::value ? __ldcs(out + j) : 0.0;
-            __stcs(out + j, spg_apply<OP>(x, y, f, g));
+            __stcs(out + j, spg_apply<OP>(x, y, fac));
         }
     }
 }

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -86,10 +87,41 @@ int spg_fold(int rank, const int *dims, const int *perm, Folded *out) {
     return SPAGHETTY_OK;
 }
 
+// Factor class: 0 = one, 1 = minus one, 2 = +-2^k, 3 = any other value.
+static int factor_class(double f, int *kout) {
+    *kout = 0;
+    if (f == 1.0) return 0;
+    if (f == -1.0) return 1;
+    if (!std::isfinite(f) || f == 0.0) return 3;
+    int e = 0;
+    const double m = std::frexp(f, &e);     // f = m * 2^e, |m| in [0.5, 1)
+    if (std::fabs(m) == 0.5 && e - 1 >= -1100 && e - 1 <= 1100) {
+        *kout = e - 1;
+        return 2;
+    }
+    return 3;
+}
+
 int spg_choose_op(double f, double g) {
-    if (g == 0.0) return f == 1.0 ? OP_COPY : OP_SCALE;
-    if (g == 1.0) return f == 1.0 ? OP_ACC1 : OP_ACCF;
+    int k;
+    const int fc = factor_class(f, &k);
+    if (g == 0.0) return OP_SORT_ONE + fc;
+    if (g == 1.0) return OP_ACC_ONE + fc;
     return OP_GEN;
+}
+
+SpgFactor spg_make_factor(double f, double g) {
+    SpgFactor F;
+    std::memset(&F, 0, sizeof(F));
+    F.f = f;
+    F.g = g;
+    int k = 0;
+    if (factor_class(f, &k) == 2) {
+        F.k = k;
+        F.kshift = (int64_t)((uint64_t)(int64_t)k << 52);
+        F.sgn = std::signbit(f) ? 0x8000000000000000ull : 0ull;
+    }
+    return F;
 }
 
 // ---------------------------------------------------------------------------
@@ -144,8 +176,10 @@ int64_t largest_divisor_le(int64_t D, int64_t v) {
 static const int kTRun = 32;      // minimum contiguous doubles per box row
 static const int kVMax = 4096;    // largest box (512 threads x 8)
 static const int kDefaultStages = 3;
+static const int kBatchThreads = 256;
+static const int kBatchEpt = 8;
 
-static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L) {
+static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L, int vmax) {
     for (int d = 0; d < s.R; ++d) L[d] = 1;
     // phase 1: both runs >= kTRun (or the whole extent of that side)
     for (int it = 0; it < 64; ++it) {
@@ -161,7 +195,7 @@ static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L) {
             break;
         }
         int64_t nl = split_len(s.D[d], need);
-        if (vol / L[d] * nl > kVMax) nl = std::max<int64_t>(L[d], kVMax * L[d] / vol);
+        if (vol / L[d] * nl > vmax) nl = std::max<int64_t>(L[d], vmax * L[d] / vol);
         if (nl <= L[d]) break;
         L[d] = nl;
     }
@@ -181,7 +215,7 @@ static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L) {
         if (d < 0) break;
         int64_t want = std::min<int64_t>(L[d] * 2, L[d] * std::max<int64_t>(2, target / vol));
         int64_t nl = split_len(s.D[d], want);
-        if (vol / L[d] * nl > kVMax) nl = largest_divisor_le(s.D[d], kVMax * L[d] / vol);
+        if (vol / L[d] * nl > vmax) nl = largest_divisor_le(s.D[d], vmax * L[d] / vol);
         if (nl <= L[d]) break;
         L[d] = nl;
     }
@@ -271,7 +305,7 @@ int spg_plan(const Folded &fo, int op, const int *box_override, int threads_over
         for (int d = 0; d < R; ++d) if (s.D[d] % L[d]) ++np;
         if (np > 2) return SPAGHETTY_ERR_CONFIG;
     } else {
-        choose_box(s, fo.nelem, num_sms, L);
+        choose_box(s, fo.nelem, num_sms, L, kVMax);
     }
     int64_t vol = volume(s, L);
     if (vol > kVMax) return SPAGHETTY_ERR_CONFIG;
@@ -298,13 +332,49 @@ int spg_plan(const Folded &fo, int op, const int *box_override, int threads_over
     return SPAGHETTY_OK;
 }
 
+// Plan for one sort of a batch: the persistent batched kernel runs every
+// sort with one CTA shape (256 threads x 8 elements), so boxes are capped at
+// 2048 elements, and a rank <= 1 problem becomes a 1-D direct box.
+int spg_plan_batch(const Folded &fo, int op, Plan *pl) {
+    std::memset(pl, 0, sizeof(*pl));
+    pl->fo = fo;
+    pl->op = op;
+    if (fo.empty) { pl->kind = KIND_EMPTY; return SPAGHETTY_OK; }
+    pl->threads = kBatchThreads;
+    pl->ept = kBatchEpt;
+    pl->stages = 0;
+    const int vmax = kBatchThreads * kBatchEpt;
+    if (fo.rank <= 1) {
+        pl->fo.rank = 1;
+        pl->fo.D[0] = fo.nelem;
+        pl->fo.P[0] = 0;
+        pl->box[0] = (int)std::min<int64_t>(fo.nelem, vmax);
+        pl->kind = KIND_DIRECT;
+        pl->run_in = pl->run_out = pl->box[0];
+        return SPAGHETTY_OK;
+    }
+    const int R = fo.rank;
+    Shape s;
+    s.R = R;
+    for (int d = 0; d < R; ++d) { s.D[d] = fo.D[d]; s.in_order[d] = R - 1 - d; }
+    for (int q = 0; q < R; ++q) s.out_order[q] = fo.P[R - 1 - q];
+    int64_t L[SPG_MAXR];
+    // many sorts share the GPU, so aim for full-size boxes
+    choose_box(s, (int64_t)1 << 40, 1, L, vmax);
+    for (int d = 0; d < R; ++d) pl->box[d] = (int)L[d];
+    pl->run_in = (int)run_len(s, L, s.in_order);
+    pl->run_out = (int)run_len(s, L, s.out_order);
+    const bool same_fastest = (fo.P[R - 1] == R - 1);
+    pl->kind = (same_fastest && L[R - 1] >= kTRun) ? KIND_DIRECT : KIND_TILED;
+    return volume(s, L) <= vmax ? SPAGHETTY_OK : SPAGHETTY_ERR_CONFIG;
+}
+
 // ---------------------------------------------------------------------------
 // Kernel parameter block.
 int spg_build_params(Plan *pl, double f, double g) {
     KParams &kp = pl->kp;
     std::memset(&kp, 0, sizeof(kp));
-    kp.f = f;
-    kp.g = g;
+    kp.fac = spg_make_factor(f, g);
     if (pl->kind == KIND_EMPTY) return SPAGHETTY_OK;
     if (pl->kind == KIND_FLAT) { kp.nelem = pl->fo.nelem; return SPAGHETTY_OK; }
     const Folded &fo = pl->fo;
@@ -329,6 +399,9 @@ int spg_build_params(Plan *pl, double f, double g) {
             else return SPAGHETTY_ERR_CONFIG;
         }
     pl->masked = (pA >= 0);
+    // the per-box limit arithmetic of masked dims is 32-bit
+    if ((pA >= 0 && fo.D[pA] > INT32_MAX / 2) || (pB >= 0 && fo.D[pB] > INT32_MAX / 2))
+        return SPAGHETTY_ERR_NOKERNEL;
     kp.lenA = pA >= 0 ? pl->box[pA] : 1;
     kp.extA = pA >= 0 ? (int32_t)fo.D[pA] : 1;
     kp.lenB = pB >= 0 ? pl->box[pB] : 1;

@@ -57,6 +57,16 @@ struct BoxGrid {
     int8_t  mpos[SPG_MAXR];       // 1 = partial dim A, 2 = partial dim B
 };
 
+// The factors of one call.  f = +-2^k is applied by exponent arithmetic where
+// that is exact (kshift = k << 52, sgn = sign bit of f); see spg_pow2.
+struct SpgFactor {
+    double f, g;
+    int64_t kshift;
+    uint64_t sgn;
+    int32_t k;
+    int32_t pad_;
+};
+
 struct KParams {
     BoxWalk ld;                   // load phase: input order
     BoxWalk st;                   // store phase: output order
@@ -68,21 +78,33 @@ struct KParams {
     int32_t stage;                // staging-tile stride in elements (pipelined kernel)
     int32_t lenA, extA;           // partial dim A: box length and extent (or 1,1)
     int32_t lenB, extB;
-    double f, g;
+    SpgFactor fac;
 };
 
 enum SpgKind { KIND_EMPTY = 0, KIND_FLAT = 1, KIND_DIRECT = 2, KIND_TILED = 3 };
 
-// Arithmetic applied per element (the reference generated nests' five cases,
-// trunk/generator2.py:57-130, plus the accumulate with an exact factor).
+// Arithmetic applied per element: the reference generated nests' cases
+// (trunk/generator2.py:57-130: copy, scale, add, scaled add, g*s + f*u),
+// with the factor split by how it can be applied.  GB300 executes FP64 at a
+// small fraction of its integer rate, so factors whose product is exact
+// (f = 1, -1, +-2^k) are applied with integer operations on the bit pattern
+// wherever that gives the same bits as the rounded multiply, and with the
+// multiply otherwise (zero, subnormal, inf/NaN inputs, over/underflow).
 enum SpgOp {
-    OP_COPY = 0,    // s = u                       (factor == 1, sort)
-    OP_SCALE = 1,   // s = u*f                     (sort)
-    OP_ACC1 = 2,    // s = s + u                   (factor == 1, sortacc)
-    OP_ACCF = 3,    // s = s + u*f                 (sortacc)
-    OP_GEN = 4,     // s = g*s + f*u               (general acc_factor)
-    OP_COUNT = 5
+    OP_SORT_ONE = 0,   // s = u
+    OP_SORT_NEG = 1,   // s = -u
+    OP_SORT_POW2 = 2,  // s = u * (+-2^k)
+    OP_SORT_ANY = 3,   // s = u * f
+    OP_ACC_ONE = 4,    // s = s + u
+    OP_ACC_NEG = 5,    // s = s + (-u)
+    OP_ACC_POW2 = 6,   // s = s + u * (+-2^k)
+    OP_ACC_ANY = 7,    // s = s + u * f
+    OP_GEN = 8,        // s = g*s + f*u
+    OP_COUNT = 9
 };
+
+// 0 = sort, 1 = sortacc, 2 = general acc_factor
+inline int spg_op_class(int op) { return op < OP_ACC_ONE ? 0 : (op == OP_GEN ? 2 : 1); }
 
 struct Folded {
     int rank;                 // folded rank (0 = single element or empty)
@@ -111,5 +133,7 @@ int spg_fold(int rank, const int *dims, const int *perm, Folded *out);
 int spg_choose_op(double f, double g);
 int spg_plan(const Folded &fo, int op, const int *box_override, int threads_override,
              int ept_override, int stages_override, int num_sms, Plan *out);
+int spg_plan_batch(const Folded &fo, int op, Plan *out);
 int spg_build_params(Plan *pl, double f, double g);
+SpgFactor spg_make_factor(double f, double g);
 int spg_selftest_host(void);

@@ -4,8 +4,9 @@ The reference generates one Fortran/C loop nest per (permutation, loop order)
 and lets a tuner pick the fastest (trunk/generator2.py:48-443 emitters,
 trunk/generator2.py:446-629 tuner).  Here the search space is not the loop
 order but the shape of the staging box and the CTA that moves it, so the
-generator emits, for every arithmetic case (the generated nests' five
-(factor, acc_factor) cases, trunk/generator2.py:57-130), every kernel family
+generator emits, for every arithmetic case (the generated nests'
+(factor, acc_factor) cases, trunk/generator2.py:57-130, with the factor split
+into 1, -1, +-2^k and any other value), every kernel family
 at every (threads, elements-per-thread) point the planner and the autotuner
 may pick.  Each output file holds one arithmetic case so that the build can
 compile them in parallel; each exposes a table of (kind, op, threads, ept,
@@ -15,7 +16,8 @@ from __future__ import annotations
 
 import os
 
-OPS = {0: "OP_COPY", 1: "OP_SCALE", 2: "OP_ACC1", 3: "OP_ACCF", 4: "OP_GEN"}
+OPS = {0: "OP_SORT_ONE", 1: "OP_SORT_NEG", 2: "OP_SORT_POW2", 3: "OP_SORT_ANY",
+       4: "OP_ACC_ONE", 5: "OP_ACC_NEG", 6: "OP_ACC_POW2", 7: "OP_ACC_ANY", 8: "OP_GEN"}
 THREADS = (128, 256, 512)
 EPTS = (1, 2, 4, 8)
 FLAT_VEC = (1, 2)

@@ -1,0 +1,161 @@
+"""Batched persistent kernel through the C ABI: bit-exact against the oracle
+and against the one-launch-per-sort path, CUDA-graph replay, and host-side
+fault injection (a poisoned work-list entry is flagged, skipped, and leaves
+every other sort correct)."""
+import random
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spaghetty_gb300.workloads import batched_mix
+from tests._util import bits_equal, first_mismatch
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def make_jobs(specs, cuda, seed=0):
+    """Device tensors + host copies for a list of job specs."""
+    jobs, host = [], []
+    for i, sp in enumerate(specs):
+        n = int(np.prod(sp["dims"]))
+        u = O.fixture_values(n, seed + 2 * i)
+        y = O.fixture_values(n, seed + 2 * i + 1)
+        du = torch.from_numpy(u).to(cuda)
+        ds = torch.from_numpy(y).to(cuda)
+        g = sp.get("g", 1.0 if sp.get("acc") else 0.0)
+        jobs.append((du, ds, sp["dims"], sp["perm"], sp["factor"], g))
+        host.append((u, y, g))
+    return jobs, host
+
+
+def small_specs(n, seed):
+    rnd = random.Random(seed)
+    specs = []
+    for _ in range(n):
+        if rnd.random() < 0.7:
+            dims = tuple(rnd.randint(3, 13) for _ in range(4))
+        else:
+            dims = tuple(rnd.randint(2, 6) for _ in range(6))
+        perm = list(range(1, len(dims) + 1))
+        rnd.shuffle(perm)
+        g = rnd.choice([0.0, 1.0, 1.0, -0.75])
+        specs.append({"dims": dims, "perm": tuple(perm), "factor": rnd.uniform(-1, 1), "g": g})
+    return specs
+
+
+def expect(spec, u, y, g, times=1):
+    out = y
+    for _ in range(times):
+        out = O.np_sort(u, spec["dims"], spec["perm"], spec["factor"], g, out=out)
+    return out
+
+
+def test_batched_matches_oracle(cuda):
+    from spaghetty_gb300.batched import Batch
+    specs = small_specs(160, 1)
+    jobs, host = make_jobs(specs, cuda, 100)
+    b = Batch(jobs)
+    info = b.info()
+    assert info["jobs"] == 160 and info["units"] >= 160
+    b.launch()
+    assert b.status() == 0
+    for sp, (du, ds, *_), (u, y, g) in zip(specs, jobs, host):
+        got = ds.cpu().numpy()
+        want = expect(sp, u, y, g)
+        assert bits_equal(got, want), (sp, first_mismatch(got, want))
+
+
+def test_batched_equals_plain_and_graph_replay(cuda):
+    from spaghetty_gb300.batched import Batch
+    specs = small_specs(96, 2)
+    jobs_a, host = make_jobs(specs, cuda, 300)
+    jobs_b, _ = make_jobs(specs, cuda, 300)
+    ba = Batch(jobs_a)
+    bb = Batch(jobs_b)
+    ba.capture()            # warm-up launch inside capture() runs once
+    ba.replay()             # ... and the replay a second time
+    bb.launch_plain()
+    bb.launch_plain()
+    assert ba.status() == 0
+    torch.cuda.synchronize()
+    for sp, ja, jb, (u, y, g) in zip(specs, jobs_a, jobs_b, host):
+        a = ja[1].cpu().numpy()
+        assert bits_equal(a, jb[1].cpu().numpy()), sp
+        assert bits_equal(a, expect(sp, u, y, g, times=2)), sp
+
+
+def test_poisoned_entry_is_flagged_and_skipped(cuda):
+    from spaghetty_gb300.batched import Batch
+    specs = small_specs(40, 3)
+    jobs, host = make_jobs(specs, cuda, 500)
+    b = Batch(jobs)
+    b.poison(7)
+    b.launch()
+    assert b.status() == 11          # SPAGHETTY_ERR_DEVICE
+    assert b.status() == 0           # the status word was cleared by the read
+    for i, (sp, (du, ds, *_), (u, y, g)) in enumerate(zip(specs, jobs, host)):
+        got = ds.cpu().numpy()
+        if i == 7:
+            assert bits_equal(got, y)        # untouched
+        else:
+            assert bits_equal(got, expect(sp, u, y, g)), i
+
+
+def test_invalid_entries_rejected_on_host(cuda):
+    from spaghetty_gb300 import SpaghettyError
+    from spaghetty_gb300.batched import Batch
+    a = torch.zeros(16, dtype=torch.float64, device=cuda)
+    c = torch.zeros(16, dtype=torch.float64, device=cuda)
+    with pytest.raises(SpaghettyError) as ei:
+        Batch([(a, c, (2, 2, 2, 2), (1, 2, 3, 4), 1.0, 0.0),
+               (a, c, (2, 2, 2, 2), (1, 1, 3, 4), 1.0, 0.0)])
+    assert ei.value.code == 2 and "entry 1" in str(ei.value)
+    with pytest.raises(SpaghettyError) as ei:           # two outputs overlap
+        Batch([(a, c, (2, 2, 2, 2), (2, 1, 3, 4), 1.0, 0.0),
+               (a, c, (2, 2, 2, 2), (4, 3, 2, 1), 1.0, 0.0)])
+    assert ei.value.code == 6
+    h = torch.zeros(16, dtype=torch.float64)
+    with pytest.raises(SpaghettyError) as ei:           # host pointer
+        Batch([(h, c, (2, 2, 2, 2), (2, 1, 3, 4), 1.0, 0.0)])
+    assert ei.value.code == 8
+
+
+def test_shared_input_is_allowed(cuda):
+    """The nine triples sortaccs read different sources, but one source may
+    feed several sorts: inputs may be shared, outputs may not."""
+    from spaghetty_gb300.batched import Batch
+    dims = (5, 6, 4, 7, 3, 5)
+    n = int(np.prod(dims))
+    u = O.fixture_values(n, 900)
+    du = torch.from_numpy(u).to(cuda)
+    perms = [(3, 2, 6, 1, 5, 4), (6, 5, 4, 3, 2, 1), (2, 6, 1, 5, 4, 3)]
+    outs = [torch.zeros(n, dtype=torch.float64, device=cuda) for _ in perms]
+    b = Batch([(du, o, dims, p, -0.5, 0.0) for o, p in zip(outs, perms)])
+    b.launch()
+    assert b.status() == 0
+    for o, p in zip(outs, perms):
+        assert bits_equal(o.cpu().numpy(), O.np_sort(u, dims, p, -0.5))
+
+
+def test_mix_4096_reduced_extents(cuda):
+    """The batched configuration's shape (4096 sorts, 70% rank 4 / 30% rank 6,
+    random perms and factors, half sortacc) at reduced extents: batched ==
+    plain bitwise on every sort, and 64 sorts checked against the oracle."""
+    from spaghetty_gb300.batched import Batch
+    mix = batched_mix(4096, seed=11, ext4=(4, 14), ext6=(3, 7))
+    specs = [{"dims": m["dims"], "perm": m["perm"], "factor": m["factor"],
+              "g": 1.0 if m["acc"] else 0.0} for m in mix]
+    ja, host = make_jobs(specs, cuda, 7000)
+    jb = [(u, s.clone(), d, p, f, g) for (u, s, d, p, f, g) in ja]
+    Batch(ja).launch()
+    pb = Batch(jb)
+    pb.launch_plain()
+    torch.cuda.synchronize()
+    for x, y in zip(ja, jb):
+        assert torch.equal(x[1], y[1])
+    rnd = random.Random(5)
+    for i in rnd.sample(range(4096), 64):
+        u, y, g = host[i]
+        assert bits_equal(ja[i][1].cpu().numpy(), expect(specs[i], u, y, g)), i
