@@ -1,0 +1,76 @@
+"""Differentiable tensor sorts.
+
+``permute_sum(x, perms, factors)`` computes y = sum_k f_k * permute_k(x)
+as one sort followed by sortaccs, in k order (each term's product rounded,
+then each sum rounded), with the GPU kernels.  Its backward is the adjoint
+of a permutation: dx = sum_k f_k * permute_{p_k^-1}(dy), computed by the
+same kernels as one sort and sortaccs with the inverse permutations -- the
+reference's sortacc (trunk/old_sort.f:512-575) applied to the incoming
+gradient.  ``permute_k`` follows the reference convention: the output holds
+x's index p_q in position q, i.e. ``x.permute(p - 1)`` (1-based p).
+"""
+from __future__ import annotations
+
+from typing import Sequence
+
+import torch
+
+from .sort import permuted_shape, sort_generic
+
+
+def inverse(perm: Sequence[int]) -> tuple:
+    inv = [0] * len(perm)
+    for q, p in enumerate(perm):
+        inv[p - 1] = q + 1
+    return tuple(inv)
+
+
+def _chain(x: torch.Tensor, perms, factors, out_shape) -> torch.Tensor:
+    """sum_k f_k * permute_k(x) by one sort and len-1 sortaccs."""
+    y = torch.empty(out_shape, dtype=x.dtype, device=x.device)
+    xs = x.contiguous()
+    for k, (p, f) in enumerate(zip(perms, factors)):
+        sort_generic(xs, y, tuple(xs.shape), p, float(f), 0.0 if k == 0 else 1.0)
+    return y
+
+
+class PermuteSum(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, perms, factors):
+        perms = tuple(tuple(int(v) for v in p) for p in perms)
+        factors = tuple(float(f) for f in factors)
+        shapes = {permuted_shape(x.shape, p) for p in perms}
+        if len(shapes) != 1:
+            raise ValueError("every permuted shape must agree, got %s" % sorted(shapes))
+        ctx.perms = perms
+        ctx.factors = factors
+        ctx.in_shape = tuple(x.shape)
+        return _chain(x, perms, factors, shapes.pop())
+
+    @staticmethod
+    def backward(ctx, dy):
+        dx = _chain(dy.contiguous(), [inverse(p) for p in ctx.perms], ctx.factors, ctx.in_shape)
+        return dx, None, None
+
+
+def permute_sum(x: torch.Tensor, perms, factors) -> torch.Tensor:
+    """y = sum_k factors[k] * x.permute(perms[k] - 1), differentiable."""
+    return PermuteSum.apply(x, perms, factors)
+
+
+def permute(x: torch.Tensor, perm: Sequence[int], factor: float = 1.0) -> torch.Tensor:
+    """factor * x.permute(perm - 1) materialised by the GPU kernels,
+    differentiable (the backward is the inverse-permutation sort)."""
+    return PermuteSum.apply(x, [tuple(perm)], [factor])
+
+
+def reference_grad(dy: torch.Tensor, perms, factors) -> torch.Tensor:
+    """The torch.permute reference gradient built the same way on the CPU:
+    dx = f_1*dy.permute(inv_1), then dx = dx + f_k*dy.permute(inv_k)
+    (separate multiply and add, FP64)."""
+    dyc = dy.detach().cpu()
+    dx = None
+    for p, f in zip(perms, factors):
+        term = torch.mul(dyc.permute([v - 1 for v in inverse(p)]), f)
+        dx = term.contiguous() if dx is None else torch.add(dx, term)
+    return dx

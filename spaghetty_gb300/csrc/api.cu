@@ -18,6 +18,7 @@
 #include <map>
 #include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 const SpgKernelEntry *spg_kernels_op0(int *n);
@@ -112,8 +113,50 @@ std::string tune_key(const Folded &fo, int op) {
 
 void autoload_tune_file();
 
+// Plans are cached by (rank, dims, perm, op, SM count): NWChem repeats the
+// same few shapes thousands of times, and planning (box search, pad
+// simulation) costs microseconds.  Cleared whenever an override changes.
+std::unordered_map<std::string, Plan> g_plans;
+std::mutex g_plans_mu;
+
+std::string plan_key(int rank, const int *dims, const int *perm, int op, int sms) {
+    std::string k;
+    k.reserve(96);
+    k += std::to_string(rank) + ":" + std::to_string(op) + ":" + std::to_string(sms) + ":";
+    for (int q = 0; q < rank; ++q) k += std::to_string(dims[q]) + ",";
+    k += ":";
+    for (int q = 0; q < rank; ++q) k += std::to_string(perm[q]) + ",";
+    return k;
+}
+
+int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
+                       Plan *pl);
+
 int make_plan(int rank, const int *dims, const int *perm, double f, double g, int sms, Plan *pl) {
     autoload_tune_file();
+    if (rank < 1 || rank > SPG_MAXR || !dims || !perm) return make_plan_uncached(rank, dims, perm, f, g, sms, pl);
+    const int op = spg_choose_op(f, g);
+    const std::string key = plan_key(rank, dims, perm, op, sms);
+    {
+        std::lock_guard<std::mutex> lk(g_plans_mu);
+        auto it = g_plans.find(key);
+        if (it != g_plans.end()) {
+            *pl = it->second;
+            pl->kp.fac = spg_make_factor(f, g);
+            return SPAGHETTY_OK;
+        }
+    }
+    int rc = make_plan_uncached(rank, dims, perm, f, g, sms, pl);
+    if (rc == SPAGHETTY_OK) {
+        std::lock_guard<std::mutex> lk(g_plans_mu);
+        if (g_plans.size() > 8192) g_plans.clear();
+        g_plans[key] = *pl;
+    }
+    return rc;
+}
+
+int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
+                       Plan *pl) {
     Folded fo;
     int rc = spg_fold(rank, dims, perm, &fo);
     if (rc) return rc;
@@ -560,8 +603,12 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
 int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const int *box,
                        int threads, int ept, int stages) {
     if (!box) {
-        std::lock_guard<std::mutex> lk(g_mu);
-        g_tune.clear();
+        {
+            std::lock_guard<std::mutex> lk(g_mu);
+            g_tune.clear();
+        }
+        std::lock_guard<std::mutex> lk2(g_plans_mu);
+        g_plans.clear();
         return SPAGHETTY_OK;
     }
     Folded fo;
@@ -583,8 +630,12 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     ov.threads = threads;
     ov.ept = ept;
     ov.stages = stages;
-    std::lock_guard<std::mutex> lk(g_mu);
-    g_tune[tune_key(fo, opc)] = ov;
+    {
+        std::lock_guard<std::mutex> lk(g_mu);
+        g_tune[tune_key(fo, opc)] = ov;
+    }
+    std::lock_guard<std::mutex> lk2(g_plans_mu);
+    g_plans.clear();
     return SPAGHETTY_OK;
 }
 

@@ -26,21 +26,30 @@
 // -- integer operations only.  Every other input (zero, subnormal, inf,
 // NaN) or result (overflow, underflow) takes the rounded multiply, so the
 // bits always equal __dmul_rn(x, f).
+// The fallback multiply sits behind a warp vote so that it is a real
+// (warp-uniform) branch, taken only by warps that hold an inexact case,
+// rather than a multiply computed for every element and then discarded.
 __device__ __forceinline__ double spg_pow2(double x, const SpgFactor &F) {
     const uint64_t b = (uint64_t)__double_as_longlong(x);
     const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
-    if (e - 1u < 2046u && (uint32_t)((int32_t)e + F.k) - 1u < 2046u)
-        return __longlong_as_double((long long)((b + (uint64_t)F.kshift) ^ F.sgn));
-    return __dmul_rn(x, F.f);
+    const bool exact = e - 1u < 2046u && (uint32_t)((int32_t)e + F.k) - 1u < 2046u;
+    double r = __longlong_as_double((long long)((b + (uint64_t)F.kshift) ^ F.sgn));
+    if (__any_sync(__activemask(), !exact)) {
+        if (!exact) r = __dmul_rn(x, F.f);
+    }
+    return r;
 }
 
 // x * -1: the sign bit flipped (exact for every non-NaN x, inf included);
 // NaN takes the multiply.
 __device__ __forceinline__ double spg_neg(double x, const SpgFactor &F) {
     const uint64_t b = (uint64_t)__double_as_longlong(x);
-    if ((b & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull)
-        return __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
-    return __dmul_rn(x, F.f);
+    const bool exact = (b & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
+    double r = __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
+    if (__any_sync(__activemask(), !exact)) {
+        if (!exact) r = __dmul_rn(x, F.f);
+    }
+    return r;
 }
 
 template <int OP>
@@ -59,11 +68,12 @@ __device__ __forceinline__ double spg_apply(double x, double y, const SpgFactor 
 template <int OP>
 struct spg_reads_out { static constexpr bool value = (OP >= OP_ACC_ONE); };
 
-// Input is read once (read-only path); outputs use the default write-back
-// policy so that L2 merges the partial sectors two neighbouring boxes write.
-__device__ __forceinline__ double spg_ld_in(const double *p) { return __ldg(p); }
-__device__ __forceinline__ double spg_ld_out(const double *p) { return *p; }
-__device__ __forceinline__ void spg_st_out(double *p, double v) { *p = v; }
+// Every element is read once and written once: streaming (evict-first)
+// accesses.  Measured on GB300 (100^4, perm 4321): with default write-back
+// stores DRAM reads grew from 1.03 GB to 1.49 GB for 0.80 GB of input.
+__device__ __forceinline__ double spg_ld_in(const double *p) { return __ldcs(p); }
+__device__ __forceinline__ double spg_ld_out(const double *p) { return __ldcs(p); }
+__device__ __forceinline__ void spg_st_out(double *p, double v) { __stcs(p, v); }
 
 // Decompose a box-local element index along a walk.  Host-callable too, so
 // that spaghetty_plan_verify can replay the exact index arithmetic on the CPU.

@@ -7,7 +7,6 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
-#include <vector>
 
 static FastDiv make_fastdiv(uint32_t d) {
     FastDiv f;
@@ -246,9 +245,8 @@ static int pick_block(int vol, int *threads, int *ept) {
 // Count shared-memory wavefronts of the store phase (8-byte words: a half
 // warp is served per wavefront when its 16 words fall in distinct bank
 // pairs) for one pad choice.
-static int64_t smem_wavefronts(const Plan &pl, int pad, const std::vector<int> &e_in_of_out) {
+static int64_t smem_wavefronts(const Plan &pl, int pad, const int *e_in_of_out, int V) {
     int64_t total = 0;
-    const int V = (int)e_in_of_out.size();
     const int NT = pl.threads;
     const int nwarps = std::min(NT / 32, 8);
     for (int k = 0; k < pl.ept; ++k)
@@ -462,7 +460,7 @@ int spg_build_params(Plan *pl, double f, double g) {
     // box dim in the input-ordered tile}
     kp.pad = 0;
     if (pl->kind == KIND_TILED && kp.st.n > 0) {
-        std::vector<int> e_in(kp.vol);
+        int e_in[kVMax];   // on the stack: planning never touches the heap
         for (int e = 0; e < kp.vol; ++e) {
             int rem = e, lin = 0;
             for (int k = 0; k < kp.st.n; ++k) {
@@ -476,7 +474,7 @@ int spg_build_params(Plan *pl, double f, double g) {
         int64_t best = -1;
         for (int c : cands) {
             if (c < 0 || (c && c >= kp.vol)) continue;
-            int64_t w = smem_wavefronts(*pl, c, e_in);
+            int64_t w = smem_wavefronts(*pl, c, e_in, kp.vol);
             if (best < 0 || w < best) { best = w; kp.pad = c; }
         }
     }

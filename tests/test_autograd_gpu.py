@@ -1,0 +1,76 @@
+"""Differentiation: y = sum_k f_k * permute_k(x) over 3 seeded permutations,
+x FP64 at 24^4 and 12^6 uniform(-1,1).  The hand-written inverse-permutation
+backward is bit-exact against the torch.permute reference gradient and
+within 1e-8 relative of FP64 central finite differences (h = 1e-6) on 64
+random entries."""
+import random
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def seeded_perms(r, seed):
+    rnd = random.Random(seed)
+    out = []
+    while len(out) < 3:
+        p = list(range(1, r + 1))
+        rnd.shuffle(p)
+        if tuple(p) not in out:
+            out.append(tuple(p))
+    return out
+
+
+@pytest.mark.parametrize("dims", [(24, 24, 24, 24), (12, 12, 12, 12, 12, 12)])
+def test_backward_bit_exact_and_finite_differences(cuda, dims):
+    from spaghetty_gb300.autograd import permute_sum, reference_grad
+    r = len(dims)
+    perms = seeded_perms(r, 17 + r)
+    factors = (0.75, -1.25, 0.3)
+    g = torch.Generator().manual_seed(5 + r)
+    xh = torch.rand(dims, dtype=torch.float64, generator=g) * 2 - 1
+    wh = torch.rand(dims, dtype=torch.float64, generator=g) * 2 - 1   # loss weights
+    x = xh.to(cuda).requires_grad_(True)
+    w = wh.to(cuda)
+    y = permute_sum(x, perms, factors)
+    # forward equals the torch.permute chain exactly
+    yref = None
+    for p, f in zip(perms, factors):
+        t = torch.mul(xh.permute([v - 1 for v in p]), f)
+        yref = t.contiguous() if yref is None else torch.add(yref, t)
+    assert torch.equal(y.detach().cpu(), yref)
+    loss = (y * w).sum()
+    loss.backward()
+    gx = x.grad.detach().cpu()
+    # bit-exact against the reference gradient of the same chain (dy = w)
+    assert torch.equal(gx, reference_grad(wh, perms, factors))
+    # central finite differences on 64 random entries
+    rnd = random.Random(99)
+    flat = xh.reshape(-1)
+    h = 1e-6
+
+    def y_at(v):
+        with torch.no_grad():
+            return permute_sum(v.to(cuda), perms, factors)
+
+    worst = 0.0
+    for i in rnd.sample(range(flat.numel()), 64):
+        xp = flat.clone()
+        xm = flat.clone()
+        xp[i] += h
+        xm[i] -= h
+        # L(x+h e_i) - L(x-h e_i) with L = sum(w*y): the difference is taken
+        # elementwise before the reduction, so the sum's own rounding over
+        # all other (unchanged) terms does not swamp the O(h) difference
+        fd = float(((y_at(xp.reshape(dims)) - y_at(xm.reshape(dims))) * w).sum()) / (2 * h)
+        an = float(gx.reshape(-1)[i])
+        worst = max(worst, abs(fd - an) / max(abs(an), 1e-3))
+    assert worst < 1e-8, worst
+
+
+def test_single_permute_gradcheck(cuda):
+    from spaghetty_gb300.autograd import permute
+    x = torch.rand((3, 4, 5, 2), dtype=torch.float64, device=cuda, requires_grad=True)
+    assert torch.autograd.gradcheck(lambda v: permute(v, (3, 1, 4, 2), -0.5), (x,))
