@@ -42,6 +42,7 @@ extern "C" {
 #define SPAGHETTY_ERR_BATCH        10  /* invalid batch entry                     */
 #define SPAGHETTY_ERR_DEVICE       11  /* device-side status word reported error  */
 #define SPAGHETTY_ERR_NOKERNEL     12  /* no compiled kernel variant fits         */
+#define SPAGHETTY_ERR_TOO_LARGE    13  /* batch exceeds the fixed scratch limits  */
 
 /* ---- NWChem drop-ins (trunk/tce_sort4_switch.F:1-8; the Hirata routines in
  *      branches/spaghetty3/python/tce_sort_hirata.F:62-63,143-144 and
@@ -277,6 +278,28 @@ int spaghetty_batch_info(const spaghetty_batch *batch, int64_t *info);
 int spaghetty_batch_poison(spaghetty_batch *batch, int index);
 
 int spaghetty_batch_destroy(spaghetty_batch *batch);
+
+/* Batched sorts for callers that cannot allocate device memory -- code
+ * running while a CUDA graph is being captured (where cudaMalloc is not
+ * allowed), or inside an application that owns the whole device memory
+ * budget.  No counterpart in the reference (its sorts are host loops that
+ * need no scratch).  Runs the same persistent batched kernel as
+ * spaghetty_batch_launch, but the work list, unit counter and status word
+ * live in a 4 MiB device array that is part of this library (every GPU that
+ * loads it holds that array until exit); the caller passes only inputs and
+ * outputs, and the call allocates nothing.  Limits: at most 1024 sorts, and
+ * the work list must fit the 4 MiB: 896 bytes per sort plus 4 bytes per
+ * work unit of ~16K elements (with 1024 sorts, about 819,000 units, i.e.
+ * some 13 G elements); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The
+ * first call on a device looks up the array's device address (set-up); make
+ * that first call before any stream capture.  Every call shares the one
+ * array, which keeps the previous call's contents: the counter and status
+ * word are cleared on each call, the rest is overwritten.  The call is
+ * synchronous on `stream` (it returns after the sorts finish, with
+ * SPAGHETTY_ERR_DEVICE if a job failed the kernel's checks); calls that
+ * overlap on the GPU (for instance from several processes' streams sharing
+ * one context) would race on the array. */
+int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries, int n, void *stream);
 
 /* Library version string. */
 const char *spaghetty_version(void);

@@ -446,6 +446,7 @@ const char *spaghetty_error_string(int code) {
         case SPAGHETTY_ERR_BATCH: return "invalid batch entry";
         case SPAGHETTY_ERR_DEVICE: return "device status word reported an error";
         case SPAGHETTY_ERR_NOKERNEL: return "no compiled kernel variant fits";
+        case SPAGHETTY_ERR_TOO_LARGE: return "batch exceeds the fixed scratch limits of the no-allocation entry";
         default: return "unknown error";
     }
 }

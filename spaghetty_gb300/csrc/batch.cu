@@ -368,3 +368,158 @@ int spaghetty_batch_destroy(spaghetty_batch *b) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Batched sorts without any allocation.
+//
+// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
+// being captured (cudaMalloc is illegal there), code that lives inside a
+// host application that owns the device memory budget (a fixed arena
+// handed out by its own allocator), or a tight loop that must not touch the
+// allocator at all.  spaghetty_sort_batch_noalloc() runs the same persistent
+// batched kernel as spaghetty_batch_create()/spaghetty_batch_launch(), but
+// its work list, unit counter and status word live in the file-scope device
+// array below, which every GPU that loads this library holds until exit.
+// The caller passes only its input and output tensors.
+#define SPG_NOALLOC_BYTES (4u << 20)          // 4 MiB of device scratch
+#define SPG_NOALLOC_MAX_SORTS 1024
+#define SPG_NOALLOC_MAX_DEVICES 64
+#define SPG_NOALLOC_JOBS_OFFSET 256u
+
+static __device__ __align__(256) unsigned char g_spg_noalloc_scratch[SPG_NOALLOC_BYTES];
+
+namespace {
+std::mutex g_na_mu;
+// Device address of g_spg_noalloc_scratch per device: in host code the
+// array's name is only a host-side stand-in, so the address is looked up once
+// per device with cudaGetSymbolAddress (with that device current).
+unsigned char *g_na_dev[SPG_NOALLOC_MAX_DEVICES];
+// Host image of the work list (static: the entry point allocates nothing).
+alignas(256) unsigned char g_na_host[SPG_NOALLOC_BYTES];
+struct NaRange { uintptr_t lo, hi; int idx; };
+NaRange g_na_outs[SPG_NOALLOC_MAX_SORTS];
+NaRange g_na_ins[SPG_NOALLOC_MAX_SORTS];
+int g_na_status;
+}  // namespace
+
+extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries, int n,
+                                            void *stream) {
+    if (n < 0 || (n > 0 && !entries)) return SPAGHETTY_ERR_NULL;
+    if (n > SPG_NOALLOC_MAX_SORTS) return SPAGHETTY_ERR_TOO_LARGE;
+    std::lock_guard<std::mutex> lk(g_na_mu);
+    g_batch_bad_index = -1;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= SPG_NOALLOC_MAX_DEVICES) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    if (!g_na_dev[dev]) {
+        // first call on this device: set-up (do it before any stream capture)
+        void *p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_spg_noalloc_scratch) != cudaSuccess || !p) {
+            cudaGetLastError();
+            return SPAGHETTY_ERR_CUDA;
+        }
+        g_na_dev[dev] = (unsigned char *)p;
+    }
+    unsigned char *dbase = g_na_dev[dev];
+    BatchJob *hjobs = reinterpret_cast<BatchJob *>(g_na_host + SPG_NOALLOC_JOBS_OFFSET);
+    uint32_t njobs = 0, nunits = 0, nouts = 0;
+    int smem_elems = 2;
+    // pass 1: validate and plan every sort into the host image
+    for (int i = 0; i < n; ++i) {
+        const spaghetty_batch_entry &e = entries[i];
+        Folded fo;
+        int rc = spg_fold(e.rank, e.dims, e.perm, &fo);
+        if (rc) { g_batch_bad_index = i; return rc; }
+        if (fo.empty) continue;
+        if (!e.unsorted || !e.sorted) { g_batch_bad_index = i; return SPAGHETTY_ERR_NULL; }
+        int du = -1, ds = -1;
+        if (!is_device_ptr(e.unsorted, &du) || !is_device_ptr(e.sorted, &ds) || du != dev || ds != dev) {
+            g_batch_bad_index = i;
+            return SPAGHETTY_ERR_MEMSPACE;
+        }
+        Plan pl;
+        const int op = spg_choose_op(e.factor, e.acc_factor);
+        rc = spg_plan_batch(fo, op, &pl);
+        if (!rc) rc = spg_build_params(&pl, e.factor, e.acc_factor);
+        if (rc) { g_batch_bad_index = i; return rc; }
+        const uintptr_t nb = (uintptr_t)fo.nelem * sizeof(double);
+        g_na_outs[nouts] = {(uintptr_t)e.sorted, (uintptr_t)e.sorted + nb, i};
+        g_na_ins[nouts] = {(uintptr_t)e.unsorted, (uintptr_t)e.unsorted + nb, i};
+        ++nouts;
+        BatchJob &j = hjobs[njobs];
+        std::memset(&j, 0, sizeof(j));
+        j.kp = pl.kp;
+        j.in = e.unsorted;
+        j.out = e.sorted;
+        j.kind = pl.kind;
+        j.op = op;
+        j.chunk = (uint32_t)std::max(1, SPG_BATCH_UNIT_ELEMS / std::max(1, (int)pl.kp.vol));
+        j.ubeg = nunits;
+        nunits += (pl.kp.ntiles + j.chunk - 1) / j.chunk;
+        if (pl.kind == KIND_TILED)
+            smem_elems = std::max(smem_elems, pl.kp.vol + (pl.kp.pad ? pl.kp.vol / pl.kp.pad + 1 : 0));
+        ++njobs;
+    }
+    // the unit map follows the job records
+    const size_t units_off = (SPG_NOALLOC_JOBS_OFFSET + (size_t)njobs * sizeof(BatchJob) + 255) & ~(size_t)255;
+    const size_t used = units_off + (size_t)nunits * sizeof(uint32_t);
+    if (used > SPG_NOALLOC_BYTES) return SPAGHETTY_ERR_TOO_LARGE;
+    uint32_t *hunits = reinterpret_cast<uint32_t *>(g_na_host + units_off);
+    for (uint32_t q = 0; q < njobs; ++q) {
+        const uint32_t units = (hjobs[q].kp.ntiles + hjobs[q].chunk - 1) / hjobs[q].chunk;
+        for (uint32_t u = 0; u < units; ++u) hunits[hjobs[q].ubeg + u] = q;
+    }
+    // outputs pairwise disjoint and disjoint from every input (in-place sort)
+    std::sort(g_na_outs, g_na_outs + nouts, [](const NaRange &a, const NaRange &b) { return a.lo < b.lo; });
+    for (uint32_t q = 1; q < nouts; ++q)
+        if (g_na_outs[q].lo < g_na_outs[q - 1].hi) { g_batch_bad_index = g_na_outs[q].idx; return SPAGHETTY_ERR_ALIAS; }
+    for (uint32_t q = 0; q < nouts; ++q) {
+        const NaRange *it = std::upper_bound(g_na_outs, g_na_outs + nouts, g_na_ins[q].lo,
+                                             [](uintptr_t v, const NaRange &r) { return v < r.hi; });
+        if (it != g_na_outs + nouts && it->lo < g_na_ins[q].hi) {
+            g_batch_bad_index = g_na_ins[q].idx;
+            return SPAGHETTY_ERR_ALIAS;
+        }
+    }
+    if (nunits == 0) return SPAGHETTY_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t *counter = reinterpret_cast<uint32_t *>(dbase);
+    int *status = reinterpret_cast<int *>(dbase + sizeof(uint32_t));
+    const BatchJob *djobs = reinterpret_cast<const BatchJob *>(dbase + SPG_NOALLOC_JOBS_OFFSET);
+    const uint32_t *dunits = reinterpret_cast<const uint32_t *>(dbase + units_off);
+    // the counter and the status word must start at zero; the rest of the
+    // scratch still holds the previous call's work list and is overwritten
+    if (cudaMemsetAsync(dbase, 0, 2 * sizeof(uint32_t), st) != cudaSuccess ||
+        cudaMemcpyAsync(dbase + SPG_NOALLOC_JOBS_OFFSET, g_na_host + SPG_NOALLOC_JOBS_OFFSET,
+                        used - SPG_NOALLOC_JOBS_OFFSET, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    const size_t smem = (size_t)smem_elems * sizeof(double);
+    if (smem > 48 * 1024 &&
+        cudaFuncSetAttribute(spg_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    int sms = 0, nb = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 152;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_batched, SPG_BATCH_NT, smem) != cudaSuccess || nb < 1)
+        nb = 1;
+    cudaGetLastError();
+    const int grid = (int)std::min<int64_t>((int64_t)sms * nb, nunits);
+    void *args[] = {(void *)&djobs, (void *)&njobs, (void *)&dunits, (void *)&nunits,
+                    (void *)&counter, (void *)&status, (void *)&smem_elems};
+    if (cudaLaunchKernel((const void *)spg_batched, dim3(grid), dim3(SPG_BATCH_NT), args, smem, st) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    // synchronous: the status word is read back before the scratch can be reused
+    if (cudaMemcpyAsync(&g_na_status, status, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    return g_na_status ? SPAGHETTY_ERR_DEVICE : SPAGHETTY_OK;
+}
