@@ -492,7 +492,9 @@ def run_case(args):
     """One sort case, W warm-up + K timed launches (the profiling workload)."""
     import torch
     import spaghetty_gb300 as S
-    dims_s, perm_s, op_s = args.case.split(":")
+    parts = args.case.split(":")
+    dims_s, perm_s, op_s = parts[:3]
+    factor = float(parts[3]) if len(parts) > 3 else 0.5
     dims = tuple(int(x) for x in dims_s.split(","))
     perm = tuple(int(x) for x in perm_s.split(","))
     op = int(op_s)
@@ -511,7 +513,7 @@ def run_case(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        S.sort_generic(u, s, dims, perm, 0.5, g)
+        S.sort_generic(u, s, dims, perm, factor, g)
         e1.record()
         e1.synchronize()
         if r >= args.warmup:
@@ -525,7 +527,7 @@ def run_case(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", default=None,
-                    help="dims:perm:op (op 0 sort, 1 sortacc): time one case only")
+                    help="dims:perm:op[:factor] (op 0 sort, 1 sortacc; factor 0.5): time one case")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)

@@ -170,12 +170,19 @@ int spaghetty_sort(int rank, const double *unsorted, double *sorted,
 int spaghetty_last_error(void);
 const char *spaghetty_error_string(int code);
 
+/* Synchronise the current device and report (then clear) the kernels'
+ * status word: SPAGHETTY_ERR_DEVICE if a kernel gave up a bounded wait (its
+ * pipeline's transfers did not arrive in time), else SPAGHETTY_OK.  The
+ * synchronous entry points check it themselves. */
+int spaghetty_device_status(void);
+
 /* ---- plans (host only, no GPU needed) --------------------------------- */
 
 typedef struct spaghetty_plan_info {
     int kind;           /* 0 = empty, 1 = flat (rank <= 1 after folding),
                            2 = direct (fastest index unchanged),
-                           3 = tiled transpose through shared memory */
+                           3 = tiled transpose through shared memory,
+                           4 = tiled, boxes moved by TMA bulk tensor copies */
     int rank;           /* rank after dropping unit dims and fusing indices */
     int64_t dims[8];    /* folded dims, input order, last is stride-1     */
     int perm[8];        /* folded permutation, 0-based, output position -> input dim */
@@ -213,7 +220,8 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
  * with the same folded (dims, perm, op).  box[] is indexed by folded dim;
  * threads in {128,256,512}; ept in {1,2,4,8}; stages in {0,2,3} (tiled
  * kernel: 0 = register-staged, 2/3 = cp.async pipeline depth, needs
- * ept >= 2).  Pass box == NULL to clear every override.  Returns a
+ * ept >= 2) or 12/13/14 (TMA-staged kernel with 2/3/4 stages; threads in
+ * {128,256}, ept in {8,16}).  Pass box == NULL to clear every override.  Returns a
  * SPAGHETTY_* code. */
 int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op,
                        const int *box, int threads, int ept, int stages);
@@ -288,17 +296,16 @@ int spaghetty_batch_destroy(spaghetty_batch *batch);
  * live in a 4 MiB device array that is part of this library (every GPU that
  * loads it holds that array until exit); the caller passes only inputs and
  * outputs, and the call allocates nothing.  Limits: at most 1024 sorts, and
- * the work list must fit the 4 MiB: 896 bytes per sort plus 4 bytes per
- * work unit of ~16K elements (with 1024 sorts, about 819,000 units, i.e.
- * some 13 G elements); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The
- * first call on a device looks up the array's device address (set-up); make
- * that first call before any stream capture.  Every call shares the one
- * array, which keeps the previous call's contents: the counter and status
- * word are cleared on each call, the rest is overwritten.  The call is
- * synchronous on `stream` (it returns after the sorts finish, with
- * SPAGHETTY_ERR_DEVICE if a job failed the kernel's checks); calls that
- * overlap on the GPU (for instance from several processes' streams sharing
- * one context) would race on the array. */
+ * the work list must fit the 4 MiB: 896 bytes per sort plus 4 bytes per work
+ * unit of ~16K elements (with 1024 sorts, about 819,000 units, i.e. some
+ * 13 G elements); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The first call on a device looks up the array's
+ * device address (set-up); make that first call before any stream capture.
+ * Every call shares the one array, which keeps the previous call's contents:
+ * the counter and status word are cleared on each call, the rest is
+ * overwritten.  The call is synchronous on `stream` (it returns after the
+ * sorts finish, with SPAGHETTY_ERR_DEVICE if a job failed the kernel's
+ * checks); calls that overlap on the GPU (for instance from several
+ * processes' streams sharing one context) would race on the array. */
 int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries, int n, void *stream);
 
 /* Library version string. */

@@ -77,6 +77,7 @@ PROTOTYPES = {
     "spaghetty_sort": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                       c_int_p, c_int_p, ctypes.c_double, ctypes.c_double]),
     "spaghetty_last_error": (ctypes.c_int, []),
+    "spaghetty_device_status": (ctypes.c_int, []),
     "spaghetty_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "spaghetty_plan_query": (ctypes.c_int, [ctypes.c_int, c_int_p, c_int_p, ctypes.c_int,
                                             ctypes.POINTER(PlanInfo)]),

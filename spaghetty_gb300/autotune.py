@@ -31,6 +31,8 @@ DEFAULT_CACHE = os.environ.get(
 
 THREADS = (128, 256, 512)
 EPTS = (1, 2, 4, 8)
+TMA_THREADS = (128, 256)
+TMA_EPTS = (8, 16)
 VMAX = 4096
 
 
@@ -141,6 +143,15 @@ def candidates(dims: Sequence[int], perm: Sequence[int], op: int = 0):
             stages = (0,) if (p["kind"] == "direct" or ept < 2) else (0, 2, 3)
             for st in stages:
                 out.append((list(b), nt, ept, st))
+        # TMA-staged kernel (stages 12..14 = 2..4 pipeline stages); the
+        # library rejects boxes that do not fit the bulk tensor copy rules
+        if p["kind"] != "direct":
+            for nt, ept in itertools.product(TMA_THREADS, TMA_EPTS):
+                cap = nt * ept
+                if cap < vol or cap >= 2 * vol + nt:
+                    continue
+                for st in (12, 13, 14):
+                    out.append((list(b), nt, ept, st))
     return p, out
 
 

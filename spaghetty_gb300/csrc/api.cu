@@ -8,7 +8,9 @@
 #include "../../include/spaghetty_gb300.h"
 #include "kernels.cuh"
 #include "plan.h"
+#include "tma.cuh"
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <dlfcn.h>
 
@@ -130,13 +132,16 @@ std::string plan_key(int rank, const int *dims, const int *perm, int op, int sms
 }
 
 int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
-                       Plan *pl);
+                       bool allow_tma, Plan *pl);
 
-int make_plan(int rank, const int *dims, const int *perm, double f, double g, int sms, Plan *pl) {
+// allow_tma: both tensors 16-byte aligned (the bulk tensor copies' rule)
+int make_plan(int rank, const int *dims, const int *perm, double f, double g, int sms, Plan *pl,
+              bool allow_tma = true) {
     autoload_tune_file();
-    if (rank < 1 || rank > SPG_MAXR || !dims || !perm) return make_plan_uncached(rank, dims, perm, f, g, sms, pl);
+    if (rank < 1 || rank > SPG_MAXR || !dims || !perm)
+        return make_plan_uncached(rank, dims, perm, f, g, sms, allow_tma, pl);
     const int op = spg_choose_op(f, g);
-    const std::string key = plan_key(rank, dims, perm, op, sms);
+    const std::string key = plan_key(rank, dims, perm, op, sms) + (allow_tma ? "t" : "n");
     {
         std::lock_guard<std::mutex> lk(g_plans_mu);
         auto it = g_plans.find(key);
@@ -146,7 +151,7 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
             return SPAGHETTY_OK;
         }
     }
-    int rc = make_plan_uncached(rank, dims, perm, f, g, sms, pl);
+    int rc = make_plan_uncached(rank, dims, perm, f, g, sms, allow_tma, pl);
     if (rc == SPAGHETTY_OK) {
         std::lock_guard<std::mutex> lk(g_plans_mu);
         if (g_plans.size() > 8192) g_plans.clear();
@@ -156,7 +161,7 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
 }
 
 int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
-                       Plan *pl) {
+                       bool allow_tma, Plan *pl) {
     Folded fo;
     int rc = spg_fold(rank, dims, perm, &fo);
     if (rc) return rc;
@@ -168,13 +173,114 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         auto it = g_tune.find(tune_key(fo, op));
         if (it != g_tune.end()) { ov = it->second; have = true; }
     }
-    rc = have ? spg_plan(fo, op, ov.box, ov.threads, ov.ept, ov.stages, sms, pl)
-              : spg_plan(fo, op, nullptr, 0, 0, 0, sms, pl);
+    // an override with stages 12..14 asks for the TMA kernel (2..4 stages);
+    // the tiled plan underneath is built with the async kernel's shape
+    const bool want_tma = have && ov.stages >= 12;
+    if (have) {
+        rc = want_tma ? spg_plan(fo, op, ov.box, 256, 16, 0, sms, pl)
+                      : spg_plan(fo, op, ov.box, ov.threads, ov.ept, ov.stages, sms, pl);
+    } else {
+        rc = spg_plan(fo, op, nullptr, 0, 0, 0, sms, pl);
+    }
     if (rc) return rc;
-    return spg_build_params(pl, f, g);
+    rc = spg_build_params(pl, f, g);
+    if (rc) return rc;
+    if (pl->kind == KIND_TILED && allow_tma && (!have || want_tma)) {
+        // default: the TMA kernel when its unpadded tile reads at most 2-way
+        // bank conflicts in the permute step
+        const bool ok_conflicts = want_tma || pl->wf_pad0 <= 2 * pl->wf_ideal;
+        TmaLayout tl;
+        if (ok_conflicts && spg_tma_layout(*pl, 3, &tl) == SPAGHETTY_OK) {
+            const int vol = pl->kp.vol;
+            if (want_tma) {
+                if (ov.threads * ov.ept < vol) return SPAGHETTY_ERR_CONFIG;
+                pl->threads = ov.threads;
+                pl->ept = ov.ept;
+                pl->stages = ov.stages - 10;
+            } else {
+                pl->threads = vol <= 1024 ? 128 : 256;
+                pl->ept = vol <= 1024 ? 8 : (vol <= 2048 ? 8 : 16);
+                pl->stages = 3;
+            }
+            pl->kind = KIND_TMA;
+        } else if (want_tma) {
+            return SPAGHETTY_ERR_CONFIG;
+        }
+    }
+    return SPAGHETTY_OK;
 }
 
 bool aligned16(const void *p) { return ((uintptr_t)p & 15u) == 0; }
+
+// ---- TMA support ----------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// Error word for the kernels' bounded waits: pinned, mapped host memory, so
+// the host reads it after a synchronisation without a copy.
+int *g_status_host = nullptr;
+int *g_status_dev = nullptr;
+std::once_flag g_status_once;
+
+int *status_word_dev() {
+    std::call_once(g_status_once, [] {
+        void *h = nullptr;
+        if (cudaHostAlloc(&h, 256, cudaHostAllocMapped | cudaHostAllocPortable) == cudaSuccess) {
+            void *d = nullptr;
+            if (cudaHostGetDevicePointer(&d, h, 0) == cudaSuccess) {
+                g_status_host = (int *)h;
+                *g_status_host = 0;
+                g_status_dev = (int *)d;
+            }
+        }
+        cudaGetLastError();
+    });
+    return g_status_dev;
+}
+
+int encode_map(CUtensorMap *m, const double *ptr, const uint64_t *dim, const uint64_t *stride,
+               const uint32_t *box) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return SPAGHETTY_ERR_CUDA;
+    cuuint64_t gd[5], gs[4];
+    cuuint32_t bd[5], es[5];
+    for (int k = 0; k < 5; ++k) { gd[k] = dim[k]; bd[k] = box[k]; es[k] = 1; }
+    for (int k = 0; k < 4; ++k) gs[k] = stride[k + 1];
+    CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, (void *)ptr, gd, gs, bd, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? SPAGHETTY_OK : SPAGHETTY_ERR_CUDA;
+}
+
+// SPAGHETTY_ERR_DEVICE (and clear) if a kernel reported a timed-out wait.
+int take_device_status() {
+    if (g_status_host && *(volatile int *)g_status_host) {
+        *(volatile int *)g_status_host = 0;
+        return SPAGHETTY_ERR_DEVICE;
+    }
+    return SPAGHETTY_OK;
+}
+
+int tma_smem_bytes(const TmaLayout &tl, int stages) {
+    return stages * tl.tp.stage_bytes + stages * 8 + 1024;
+}
 
 int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) {
     if (pl.kind == KIND_EMPTY) return SPAGHETTY_OK;
@@ -191,6 +297,28 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
         void *args[] = {(void *)&u, (void *)&s, (void *)&n, (void *)&fac};
         pl.grid = grid;
         err = cudaLaunchKernel(k->fn, dim3(grid), dim3(256), args, 0, st);
+    } else if (pl.kind == KIND_TMA) {
+        const SpgKernelEntry *k = find_kernel(KIND_TMA, pl.op, pl.threads, pl.ept, pl.stages);
+        if (!k) return SPAGHETTY_ERR_NOKERNEL;
+        TmaLayout tl;
+        int rc = spg_tma_layout(pl, pl.stages, &tl);
+        if (rc) return rc;
+        tl.tp.status = status_word_dev();
+        alignas(64) CUtensorMap mi, mo;
+        if ((rc = encode_map(&mi, u, tl.in_dim, tl.in_stride, tl.in_box))) return rc;
+        if ((rc = encode_map(&mo, s, tl.out_dim, tl.out_stride, tl.out_box))) return rc;
+        const int smem = tma_smem_bytes(tl, pl.stages);
+        if (smem > 48 * 1024 &&
+            cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
+            cudaGetLastError();
+            return SPAGHETTY_ERR_CUDA;
+        }
+        const int occ = occupancy(k, smem);
+        int64_t grid = std::min<int64_t>((int64_t)pl.kp.ntiles, (int64_t)sms * occ);
+        if (grid < 1) grid = 1;
+        pl.grid = (int)grid;
+        void *args[] = {(void *)&mi, (void *)&mo, (void *)&pl.kp, (void *)&tl.tp};
+        err = cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(pl.threads), args, (size_t)smem, st);
     } else {
         const SpgKernelEntry *k = find_kernel(pl.kind, pl.op, pl.threads, pl.ept, pl.stages);
         if (!k) return SPAGHETTY_ERR_NOKERNEL;
@@ -289,7 +417,10 @@ int sort_sync(int rank, const double *u, double *s, const int *dims, const int *
     DeviceGuard guard(dev);
     if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
     Plan pl;
-    rc = make_plan(rank, dims, perm, f, g, device_sms(dev), &pl);
+    // staged sides use cudaMalloc'd buffers (aligned); device sides are the
+    // caller's pointers
+    const bool allow_tma = (ku == 1 ? aligned16(u) : true) && (ks == 1 ? aligned16(s) : true);
+    rc = make_plan(rank, dims, perm, f, g, device_sms(dev), &pl, allow_tma);
     if (rc) return rc;
     cudaStream_t st = 0;  // legacy default stream: ordered after prior blocking-stream work
     const size_t n = (size_t)fo.nelem;
@@ -298,7 +429,7 @@ int sort_sync(int rank, const double *u, double *s, const int *dims, const int *
         rc = launch_plan(pl, u, s, st, dev);
         if (rc) return rc;
         if (cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
-        return SPAGHETTY_OK;
+        return take_device_status();
     }
     std::lock_guard<std::mutex> lk(g_stage_mu);
     Staging &sg = g_stage[dev];
@@ -323,7 +454,7 @@ int sort_sync(int rank, const double *u, double *s, const int *dims, const int *
     if (ks == 0)
         if (cudaMemcpyAsync(s, sg.s, bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess) goto cuda_fail;
     if (cudaStreamSynchronize(st) != cudaSuccess) goto cuda_fail;
-    return SPAGHETTY_OK;
+    return take_device_status();
 cuda_fail:
     cudaGetLastError();
     cudaStreamSynchronize(st);
@@ -453,6 +584,14 @@ const char *spaghetty_error_string(int code) {
 
 int spaghetty_last_error(void) { return g_last_error; }
 
+int spaghetty_device_status(void) {
+    if (cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    return take_device_status();
+}
+
 const char *spaghetty_version(void) { return "spaghetty_gb300 0.1 (sm_103a)"; }
 
 int spaghetty_selftest(void) { return spg_selftest_host(); }
@@ -468,7 +607,8 @@ int spaghetty_sort_async(int rank, const double *unsorted, double *sorted, const
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return record(SPAGHETTY_ERR_CUDA); }
     Plan pl;
-    rc = make_plan(rank, dims, perm, factor, acc_factor, device_sms(dev), &pl);
+    rc = make_plan(rank, dims, perm, factor, acc_factor, device_sms(dev), &pl,
+                   aligned16(unsorted) && aligned16(sorted));
     if (rc) return record(rc);
     return record(launch_plan(pl, unsorted, sorted, (cudaStream_t)stream, dev));
 }
@@ -507,6 +647,83 @@ int spaghetty_plan_query(int rank, const int *dims, const int *perm, int op,
     return SPAGHETTY_OK;
 }
 
+// Replays the TMA kernel's data movement on the host: box coordinates from
+// spg_tma_coords, element positions inside the two tensor maps' boxes
+// (clipped exactly as the hardware clips: out-of-range loads read zero,
+// out-of-range stores are dropped), and the permute step's table.
+static int verify_tma(const Plan &pl, int64_t *stats) {
+    TmaLayout tl;
+    if (spg_tma_layout(pl, pl.stages, &tl)) return SPAGHETTY_ERR_CONFIG;
+    const KParams &kp = pl.kp;
+    const Folded &fo = pl.fo;
+    const int64_t n = fo.nelem;
+    if (n > ((int64_t)1 << 27)) return SPAGHETTY_ERR_CONFIG;
+    if ((int64_t)kp.vol * 8 > tl.tp.in_bytes || pl.threads * pl.ept < kp.vol) return SPAGHETTY_ERR_CONFIG;
+    const int R = fo.rank;
+    int64_t istr[SPG_MAXR];
+    {
+        int64_t s = 1;
+        for (int d = R - 1; d >= 0; --d) { istr[d] = s; s *= fo.D[d]; }
+    }
+    std::vector<int64_t> got((size_t)n, -1);
+    int64_t writes = 0;
+    for (uint32_t t = 0; t < kp.ntiles; ++t) {
+        int32_t ci[5], co[5];
+        spg_tma_coords(kp, tl.tp, t, ci, co);
+        for (int m = 0; m < 5; ++m)
+            if (ci[m] < 0 || co[m] < 0 || (uint64_t)ci[m] >= tl.in_dim[m] || (uint64_t)co[m] >= tl.out_dim[m])
+                return SPAGHETTY_ERR_CONFIG;   // every box starts inside both tensors
+        if ((ci[0] * 8) % 16 || (co[0] * 8) % 16) return SPAGHETTY_ERR_CONFIG;
+        for (uint32_t e = 0; e < (uint32_t)kp.vol; ++e) {
+            // output position of tile element e (dense over the output box)
+            int64_t rem = e, og = 0;
+            bool oin = true;
+            for (int m = 0; m < 5; ++m) {
+                const int64_t c = rem % tl.out_box[m];
+                rem /= tl.out_box[m];
+                const int64_t x = co[m] + c;
+                if ((uint64_t)x >= tl.out_dim[m]) oin = false;
+                og += x * (int64_t)(tl.out_stride[m] / 8);
+            }
+            // input position of the element the permute step reads
+            int32_t a, b, lin;
+            uint32_t pk;
+            spg_walk(kp.st, e, a, b, lin, pk);
+            if (lin < 0 || lin >= kp.vol) return SPAGHETTY_ERR_CONFIG;
+            int64_t remi = lin, ig = 0;
+            bool iin = true;
+            for (int m = 0; m < 5; ++m) {
+                const int64_t c = remi % tl.in_box[m];
+                remi /= tl.in_box[m];
+                const int64_t x = ci[m] + c;
+                if ((uint64_t)x >= tl.in_dim[m]) iin = false;
+                ig += x * (int64_t)(tl.in_stride[m] / 8);
+            }
+            if (!oin) continue;
+            if (!iin || og < 0 || og >= n || ig < 0 || ig >= n) return SPAGHETTY_ERR_CONFIG;
+            if (got[(size_t)og] != -1) return SPAGHETTY_ERR_CONFIG;
+            got[(size_t)og] = ig;
+            ++writes;
+        }
+    }
+    for (int64_t o = 0; o < n; ++o) {
+        int64_t rem = o, src = 0;
+        for (int q = R - 1; q >= 0; --q) {
+            const int64_t ext = fo.D[fo.P[q]];
+            src += (rem % ext) * istr[fo.P[q]];
+            rem /= ext;
+        }
+        if (got[(size_t)o] != src) return SPAGHETTY_ERR_CONFIG;
+    }
+    if (stats) {
+        stats[0] = writes;
+        stats[1] = writes;
+        stats[2] = kp.ntiles;
+        stats[3] = tl.tp.stage_bytes / 8;
+    }
+    return SPAGHETTY_OK;
+}
+
 int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, int num_sms,
                           int64_t *stats) {
     // Replays, on the host, the index arithmetic of the exact KParams a
@@ -518,6 +735,7 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
     if (rc) return rc;
     if (stats) for (int q = 0; q < 4; ++q) stats[q] = 0;
     if (pl.kind == KIND_EMPTY || pl.kind == KIND_FLAT) return SPAGHETTY_OK;
+    if (pl.kind == KIND_TMA) return verify_tma(pl, stats);
     const KParams &kp = pl.kp;
     const Folded &fo = pl.fo;
     const int64_t n = fo.nelem;
@@ -618,14 +836,21 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     if (fo.empty || fo.rank < 2) return SPAGHETTY_ERR_CONFIG;
     if (threads != 128 && threads != 256 && threads != 512) return SPAGHETTY_ERR_CONFIG;
     if (ept != 1 && ept != 2 && ept != 4 && ept != 8) return SPAGHETTY_ERR_CONFIG;
-    if (stages != 0 && stages != 2 && stages != 3) return SPAGHETTY_ERR_CONFIG;
+    const bool tma = stages >= 12 && stages <= 14;
+    if (stages != 0 && stages != 2 && stages != 3 && !tma) return SPAGHETTY_ERR_CONFIG;
     if (stages && ept < 2) return SPAGHETTY_ERR_CONFIG;
+    if (tma && ((threads != 128 && threads != 256) || (ept != 8 && ept != 16))) return SPAGHETTY_ERR_CONFIG;
     const int opc = op == 0 ? OP_SORT_ANY : (op == 1 ? OP_ACC_ANY : OP_GEN);
     Plan pl;
-    rc = spg_plan(fo, opc, box, threads, ept, stages, 152, &pl);
+    rc = spg_plan(fo, opc, box, tma ? 256 : threads, tma ? 16 : ept, tma ? 0 : stages, 152, &pl);
     if (rc) return rc;
     rc = spg_build_params(&pl, 0.5, 1.0);
     if (rc) return rc;
+    if (tma) {
+        TmaLayout tl;
+        if (pl.kind != KIND_TILED || threads * ept < pl.kp.vol || spg_tma_layout(pl, stages - 10, &tl))
+            return SPAGHETTY_ERR_CONFIG;
+    }
     TuneOverride ov;
     for (int d = 0; d < SPG_MAXR; ++d) ov.box[d] = d < fo.rank ? box[d] : 1;
     ov.threads = threads;

@@ -21,6 +21,14 @@
 #include <stdint.h>
 #include "plan.h"
 
+// Rounded FP64 multiply as volatile PTX: it cannot be hoisted out of the
+// rarely taken branches below and computed for every element.
+__device__ __forceinline__ double spg_dmul_branch(double x, double f) {
+    double r;
+    asm volatile("mul.rn.f64 %0, %1, %2;\n" : "=d"(r) : "d"(x), "d"(f));
+    return r;
+}
+
 // x * f for f = +-2^k: when x is normal and x*f is normal, the product is
 // exact and equals x with k added to its exponent field and f's sign applied
 // -- integer operations only.  Every other input (zero, subnormal, inf,
@@ -35,7 +43,7 @@ __device__ __forceinline__ double spg_pow2(double x, const SpgFactor &F) {
     const bool exact = e - 1u < 2046u && (uint32_t)((int32_t)e + F.k) - 1u < 2046u;
     double r = __longlong_as_double((long long)((b + (uint64_t)F.kshift) ^ F.sgn));
     if (__any_sync(__activemask(), !exact)) {
-        if (!exact) r = __dmul_rn(x, F.f);
+        if (!exact) r = spg_dmul_branch(x, F.f);
     }
     return r;
 }
@@ -47,7 +55,7 @@ __device__ __forceinline__ double spg_neg(double x, const SpgFactor &F) {
     const bool exact = (b & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
     double r = __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
     if (__any_sync(__activemask(), !exact)) {
-        if (!exact) r = __dmul_rn(x, F.f);
+        if (!exact) r = spg_dmul_branch(x, F.f);
     }
     return r;
 }

@@ -367,6 +367,27 @@ int spg_plan_batch(const Folded &fo, int op, Plan *pl) {
     return volume(s, L) <= vmax ? SPAGHETTY_OK : SPAGHETTY_ERR_CONFIG;
 }
 
+// Order of the box grid's dims, fastest-varying first.  Dims that the box
+// covers partially (1 < L < D) come first: two boxes that are neighbours
+// along such a dim share the cache lines at their common edge, and giving
+// them consecutive box indices keeps both in flight at the same time, so the
+// shared lines are fetched from DRAM once.  The remaining dims (L == 1)
+// follow, all in output order.  Returns the number of dims listed.
+static int grid_order(const Plan &pl, int *dims_out) {
+    const Folded &fo = pl.fo;
+    const int R = fo.rank;
+    int n = 0;
+    for (int pass = 0; pass < 2; ++pass)
+        for (int q = R - 1; q >= 0; --q) {
+            const int d = fo.P[q];
+            const int64_t c = (fo.D[d] + pl.box[d] - 1) / pl.box[d];
+            if (c <= 1) continue;
+            const bool partial = pl.box[d] > 1;
+            if ((pass == 0) == partial) dims_out[n++] = d;
+        }
+    return n;
+}
+
 // ---------------------------------------------------------------------------
 // Kernel parameter block.
 int spg_build_params(Plan *pl, double f, double g) {
@@ -439,13 +460,14 @@ int spg_build_params(Plan *pl, double f, double g) {
         kp.st.mpos[k] = mp(d);
     }
     if (maxoff_in > INT32_MAX || maxoff_out > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
-    // grid of boxes, output order fastest first
+    // grid of boxes (grid_order)
     int64_t ntiles = 1;
     kp.grid.n = 0;
-    for (int q = R - 1; q >= 0; --q) {
-        int d = fo.P[q];
-        int64_t c = (fo.D[d] + pl->box[d] - 1) / pl->box[d];
-        if (c <= 1) continue;
+    int gdims[SPG_MAXR];
+    const int ng = grid_order(*pl, gdims);
+    for (int gi = 0; gi < ng; ++gi) {
+        const int d = gdims[gi];
+        const int64_t c = (fo.D[d] + pl->box[d] - 1) / pl->box[d];
         int k = kp.grid.n++;
         kp.grid.cnt[k] = make_fastdiv((uint32_t)c);
         kp.grid.in_step[k] = (int64_t)pl->box[d] * istr[d];
@@ -475,7 +497,18 @@ int spg_build_params(Plan *pl, double f, double g) {
         for (int c : cands) {
             if (c < 0 || (c && c >= kp.vol)) continue;
             int64_t w = smem_wavefronts(*pl, c, e_in, kp.vol);
+            if (c == 0) pl->wf_pad0 = w;
             if (best < 0 || w < best) { best = w; kp.pad = c; }
+        }
+        // conflict-free: one wavefront per half warp of live elements
+        {
+            const int nwarps = std::min(pl->threads / 32, 8);
+            int64_t ideal = 0;
+            for (int k = 0; k < pl->ept; ++k)
+                for (int w = 0; w < nwarps; ++w)
+                    for (int h = 0; h < 2; ++h)
+                        if (k * pl->threads + w * 32 + h * 16 < kp.vol) ++ideal;
+            pl->wf_ideal = ideal;
         }
     }
     const int tile = kp.vol + (kp.pad ? kp.vol / kp.pad + 1 : 0);
@@ -505,4 +538,118 @@ int spg_selftest_host(void) {
         }
     }
     return 0;
+}
+
+// ---------------------------------------------------------------------------
+// TMA layout.  Folded dims are grouped, fastest first, into at most five
+// tensor-map dims: a slower dim joins the current group when every dim
+// already in it is covered by the box in full (the group is then one
+// contiguous range), or when it and every dim already in the group have
+// box length 1.  Box lengths along a map dim are at most 256, the innermost
+// box row is a multiple of 16 bytes, and every stride a multiple of 16 bytes
+// (the bulk tensor copy's rules); otherwise the plan is not TMA-eligible.
+static int tma_map(const Plan &pl, const int *order, const int64_t *gstride, int *nmap,
+                   uint64_t *dim, uint64_t *stride, uint32_t *box, int8_t *mdim_of,
+                   int64_t *weight_of) {
+    const Folded &fo = pl.fo;
+    const int R = fo.rank;
+    int m = -1;
+    bool group_full = false, group_unit = false;
+    for (int q = 0; q < R; ++q) {
+        const int d = order[q];
+        const int64_t D = fo.D[d];
+        const int64_t L = pl.box[d];
+        bool merge = false;
+        if (m >= 0) {
+            if (group_full) merge = true;
+            else if (group_unit && L == 1) merge = true;
+        }
+        if (merge) {
+            weight_of[d] = (int64_t)dim[m];
+            dim[m] *= (uint64_t)D;
+            box[m] = (uint32_t)((int64_t)box[m] * L);
+            group_full = group_full && (L == D);
+            group_unit = group_unit && (L == 1);
+        } else {
+            if (++m >= 5) return SPAGHETTY_ERR_NOKERNEL;
+            dim[m] = (uint64_t)D;
+            box[m] = (uint32_t)L;
+            stride[m] = (uint64_t)gstride[d] * 8u;
+            weight_of[d] = 1;
+            group_full = (L == D);
+            group_unit = (L == 1);
+        }
+        mdim_of[d] = (int8_t)m;
+    }
+    *nmap = m + 1;
+    for (int k = 0; k < *nmap; ++k) {
+        if (box[k] < 1 || box[k] > 256) return SPAGHETTY_ERR_NOKERNEL;
+        if (dim[k] > ((uint64_t)1 << 31)) return SPAGHETTY_ERR_NOKERNEL;
+        if (k > 0 && (stride[k] % 16 != 0 || stride[k] >= ((uint64_t)1 << 40))) return SPAGHETTY_ERR_NOKERNEL;
+    }
+    if (stride[0] != 8 || (box[0] * 8u) % 16u != 0) return SPAGHETTY_ERR_NOKERNEL;
+    // pad to five dims with unit dims
+    for (int k = *nmap; k < 5; ++k) {
+        dim[k] = 1;
+        box[k] = 1;
+        stride[k] = stride[k - 1] * dim[k - 1];
+        if (stride[k] >= ((uint64_t)1 << 40)) return SPAGHETTY_ERR_NOKERNEL;
+    }
+    return SPAGHETTY_OK;
+}
+
+int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out) {
+    std::memset(out, 0, sizeof(*out));
+    if (pl.kind != KIND_TILED && pl.kind != KIND_TMA && pl.kind != KIND_DIRECT) return SPAGHETTY_ERR_NOKERNEL;
+    const Folded &fo = pl.fo;
+    const int R = fo.rank;
+    if (R < 1) return SPAGHETTY_ERR_NOKERNEL;
+    int64_t istr[SPG_MAXR], ostr[SPG_MAXR];
+    {
+        int pinv[SPG_MAXR];
+        for (int q = 0; q < R; ++q) pinv[fo.P[q]] = q;
+        int64_t s = 1;
+        for (int d = R - 1; d >= 0; --d) { istr[d] = s; s *= fo.D[d]; }
+        int64_t so = 1, op[SPG_MAXR];
+        for (int q = R - 1; q >= 0; --q) { op[q] = so; so *= fo.D[fo.P[q]]; }
+        for (int d = 0; d < R; ++d) ostr[d] = op[pinv[d]];
+    }
+    int in_order[SPG_MAXR], out_order[SPG_MAXR];
+    for (int q = 0; q < R; ++q) { in_order[q] = R - 1 - q; out_order[q] = fo.P[R - 1 - q]; }
+    int8_t mi[SPG_MAXR], mo[SPG_MAXR];
+    int64_t wi[SPG_MAXR], wo[SPG_MAXR];
+    int rc = tma_map(pl, in_order, istr, &out->rank_in, out->in_dim, out->in_stride, out->in_box, mi, wi);
+    if (rc) return rc;
+    rc = tma_map(pl, out_order, ostr, &out->rank_out, out->out_dim, out->out_stride, out->out_box, mo, wo);
+    if (rc) return rc;
+    // grid dims in the order spg_build_params lists them (grid_order)
+    const KParams &kp = pl.kp;
+    int k = 0;
+    int gdims[SPG_MAXR];
+    const int ng = grid_order(pl, gdims);
+    for (int gi = 0; gi < ng; ++gi) {
+        const int d = gdims[gi];
+        const int64_t c = (fo.D[d] + pl.box[d] - 1) / pl.box[d];
+        if (k >= kp.grid.n) return SPAGHETTY_ERR_CONFIG;
+        const int64_t mul_in = (int64_t)pl.box[d] * wi[d], mul_out = (int64_t)pl.box[d] * wo[d];
+        if (mul_in * c > INT32_MAX || mul_out * c > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
+        out->tp.in_mdim[k] = mi[d];
+        out->tp.out_mdim[k] = mo[d];
+        out->tp.in_mul[k] = (int32_t)mul_in;
+        out->tp.out_mul[k] = (int32_t)mul_out;
+        ++k;
+    }
+    if (k != kp.grid.n) return SPAGHETTY_ERR_CONFIG;
+    // each bulk load delivers exactly one box: the mbarrier's transaction
+    // count must equal it
+    int64_t pin = 1, pout = 1;
+    for (int m = 0; m < 5; ++m) { pin *= out->in_box[m]; pout *= out->out_box[m]; }
+    if (pin != kp.vol || pout != kp.vol) return SPAGHETTY_ERR_NOKERNEL;
+    const int64_t tile = (int64_t)kp.vol * 8;
+    const int64_t tile_al = (tile + 1023) & ~(int64_t)1023;
+    out->tp.in_bytes = (int32_t)tile_al;
+    out->tp.stage_bytes = (int32_t)(2 * tile_al);
+    out->tp.tx_bytes = (int32_t)(tile * (spg_op_class(pl.op) == 0 ? 1 : 2));
+    (void)stages;
+    return SPAGHETTY_OK;
 }

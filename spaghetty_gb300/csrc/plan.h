@@ -81,7 +81,32 @@ struct KParams {
     SpgFactor fac;
 };
 
-enum SpgKind { KIND_EMPTY = 0, KIND_FLAT = 1, KIND_DIRECT = 2, KIND_TILED = 3 };
+enum SpgKind { KIND_EMPTY = 0, KIND_FLAT = 1, KIND_DIRECT = 2, KIND_TILED = 3, KIND_TMA = 4 };
+
+// TMA-staged kernel: how box t's tile coordinates map onto the two 5-D
+// tensor maps (input map over the folded input dims in input order, output
+// map over the folded dims in output order, adjacent dims merged where the
+// box allows).  Grid dim k adds c_k * in_mul[k] to input-map coordinate
+// in_mdim[k] (and likewise for the output map).
+struct TmaParams {
+    int8_t in_mdim[SPG_MAXR];
+    int8_t out_mdim[SPG_MAXR];
+    int32_t in_mul[SPG_MAXR];
+    int32_t out_mul[SPG_MAXR];
+    int32_t stage_bytes;          // input tile + output tile (1024-aligned each)
+    int32_t in_bytes;             // offset of the output tile within a stage
+    int32_t tx_bytes;             // bytes the loads of one box deliver
+    int32_t pad_;
+    int *status;                  // error word (bounded waits that timed out)
+};
+
+struct TmaLayout {
+    int rank_in, rank_out;        // map ranks before padding to 5
+    uint64_t in_dim[5], out_dim[5];
+    uint64_t in_stride[5], out_stride[5];   // bytes, [0] = 8 (element)
+    uint32_t in_box[5], out_box[5];
+    TmaParams tp;
+};
 
 // Arithmetic applied per element: the reference generated nests' cases
 // (trunk/generator2.py:57-130: copy, scale, add, scaled add, g*s + f*u),
@@ -125,6 +150,7 @@ struct Plan {
     int masked;
     int grid;                 // filled at launch time
     int smem_bytes;
+    int64_t wf_pad0, wf_ideal; // store-phase shared wavefronts: unpadded tile, conflict-free
     KParams kp;
 };
 
@@ -137,3 +163,7 @@ int spg_plan_batch(const Folded &fo, int op, Plan *out);
 int spg_build_params(Plan *pl, double f, double g);
 SpgFactor spg_make_factor(double f, double g);
 int spg_selftest_host(void);
+// TMA layout of a tiled plan: SPAGHETTY_OK, or SPAGHETTY_ERR_NOKERNEL when
+// the plan cannot be expressed as 5-D tensor maps (odd stride-1 extents,
+// > 5 map dims, box > 256 along a map dim, ...).  stages: pipeline depth.
+int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out);

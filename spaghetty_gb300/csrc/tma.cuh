@@ -1,0 +1,206 @@
+// tma.cuh -- the TMA-staged tiled kernel (sm_90+ bulk tensor copies; built
+// for sm_103a).
+//
+// Each box is moved global -> shared by ONE cp.async.bulk.tensor load
+// described by a tensor map over the (folded) input, and shared -> global by
+// ONE bulk tensor store described by a tensor map over the output.  The
+// hardware clips partial boxes at the tensor edges (loads zero-fill, stores
+// drop), so the kernel carries no element masks and no global address
+// arithmetic.  Threads only permute inside shared memory: element e of the
+// output-ordered tile takes element smr[e] of the input-ordered tile, with
+// the factor arithmetic applied; for sortacc the old output box is loaded
+// into the output tile by the same bulk load.
+//
+// Pipeline: S stages, each an input tile, an output tile and an mbarrier.
+// Thread 0 issues the loads S-1 boxes ahead and the stores.  Every wait on an
+// mbarrier is bounded: on timeout the kernel records an error in the status
+// word, waits (bounded) for its own loads in flight, and returns.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "kernels.cuh"
+#include "plan.h"
+
+#define SPG_TMA_WAIT_LIMIT (1u << 22)
+
+__device__ __forceinline__ void spg_mbar_init(uint32_t addr, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(addr), "r"(count) : "memory");
+}
+__device__ __forceinline__ void spg_mbar_expect_tx(uint32_t addr, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(addr), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool spg_mbar_try_wait(uint32_t addr, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false after SPG_TMA_WAIT_LIMIT polls.
+__device__ __forceinline__ bool spg_mbar_wait(uint32_t addr, uint32_t parity) {
+    for (uint32_t i = 0; i < SPG_TMA_WAIT_LIMIT; ++i)
+        if (spg_mbar_try_wait(addr, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void spg_tma_load5(uint32_t dst, const void *tmap, const int32_t *c,
+                                              uint32_t mbar) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];\n" ::"r"(dst),
+        "l"(tmap), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(mbar)
+        : "memory");
+}
+__device__ __forceinline__ void spg_tma_store5(const void *tmap, const int32_t *c, uint32_t src) {
+    asm volatile(
+        "cp.async.bulk.tensor.5d.global.shared::cta.tile.bulk_group"
+        " [%0, {%2, %3, %4, %5, %6}], [%1];\n" ::"l"(tmap),
+        "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4])
+        : "memory");
+}
+__device__ __forceinline__ void spg_bulk_commit() {
+    asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
+}
+__device__ __forceinline__ void spg_bulk_wait_read0() {
+    asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+}
+__device__ __forceinline__ void spg_bulk_wait0() {
+    asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
+}
+__device__ __forceinline__ void spg_fence_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+__device__ __forceinline__ void spg_fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+
+// Box t -> start coordinates of the box in both tensor maps.
+__host__ __device__ __forceinline__ void spg_tma_coords(const KParams &p, const TmaParams &tp,
+                                                       uint32_t t, int32_t *ci, int32_t *co) {
+#pragma unroll
+    for (int q = 0; q < 5; ++q) { ci[q] = 0; co[q] = 0; }
+#pragma unroll
+    for (int k = 0; k < SPG_MAXR; ++k) {
+        if (k < p.grid.n) {
+            const uint32_t q = fd_div(t, p.grid.cnt[k]);
+            const uint32_t c = t - q * p.grid.cnt[k].d;
+            t = q;
+#pragma unroll
+            for (int m = 0; m < 5; ++m) {
+                if (tp.in_mdim[k] == m) ci[m] += (int32_t)c * tp.in_mul[k];
+                if (tp.out_mdim[k] == m) co[m] += (int32_t)c * tp.out_mul[k];
+            }
+        }
+    }
+}
+
+template <int NT, int EPT, int OP, int S>
+__global__ void __launch_bounds__(NT)
+spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
+              const __grid_constant__ CUtensorMap tmap_out,
+              const __grid_constant__ KParams p, const __grid_constant__ TmaParams tp) {
+    extern __shared__ __align__(1024) unsigned char smem_raw0[];
+    // stage s: input tile at s*stage_bytes, output tile at s*stage_bytes +
+    // in_bytes; the base is rounded up to 1024 bytes (the launch adds 1 KB)
+    const uint32_t raw = (uint32_t)__cvta_generic_to_shared(smem_raw0);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char *smem_raw = smem_raw0 + (base - raw);
+    const uint32_t sb = (uint32_t)tp.stage_bytes;
+    const uint32_t in_bytes = (uint32_t)tp.in_bytes;
+    const uint32_t mbar0 = base + (uint32_t)S * sb;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t G = gridDim.x;
+    const uint32_t tx = (uint32_t)tp.tx_bytes;
+
+    // element tables: output-tile element e = tid + k*NT takes input-tile
+    // element smr[k]
+    int32_t smr[EPT];
+#pragma unroll
+    for (int k = 0; k < EPT; ++k) {
+        const uint32_t e = tid + k * NT;
+        smr[k] = -1;
+        if (e < (uint32_t)p.vol) {
+            int32_t a, b, lin;
+            uint32_t pk;
+            spg_walk(p.st, e, a, b, lin, pk);
+            smr[k] = lin;
+        }
+    }
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) spg_mbar_init(mbar0 + 8u * s, 1u);
+        spg_fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](uint32_t t, int s) {
+        int32_t ci[5], co[5];
+        spg_tma_coords(p, tp, t, ci, co);
+        const uint32_t mb = mbar0 + 8u * (uint32_t)s;
+        spg_mbar_expect_tx(mb, tx);
+        spg_tma_load5(base + (uint32_t)s * sb, &tmap_in, ci, mb);
+        if (spg_reads_out<OP>::value) spg_tma_load5(base + (uint32_t)s * sb + in_bytes, &tmap_out, co, mb);
+    };
+
+    if (tid == 0) {
+#pragma unroll
+        for (int q = 0; q < S - 1; ++q) {
+            const uint32_t t = blockIdx.x + (uint32_t)q * G;
+            if (t < p.ntiles) issue(t, q);
+        }
+    }
+    const SpgFactor fac = p.fac;
+    bool failed = false;
+    int it = 0;
+    for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
+        const int s = it % S;
+        if (tid == 0) {
+            const uint32_t tn = t + (uint32_t)(S - 1) * G;
+            if (tn < p.ntiles) {
+                spg_bulk_wait_read0();      // the stage's previous store has read its tile
+                issue(tn, (it + S - 1) % S);
+            }
+        }
+        const bool ok = spg_mbar_wait(mbar0 + 8u * (uint32_t)s, (uint32_t)((it / S) & 1));
+        if (__syncthreads_or(!ok)) {         // every thread leaves together
+            failed = true;
+            break;
+        }
+        const double *tin = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb);
+        double *tout = reinterpret_cast<double *>(smem_raw + (size_t)s * sb + in_bytes);
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            if (smr[k] >= 0) {
+                const uint32_t e = tid + k * NT;
+                const double y = spg_reads_out<OP>::value ? tout[e] : 0.0;
+                tout[e] = spg_apply<OP>(tin[smr[k]], y, fac);
+            }
+        }
+        spg_fence_async_smem();             // generic-proxy writes -> visible to the bulk store
+        __syncthreads();
+        if (tid == 0) {
+            int32_t ci[5], co[5];
+            spg_tma_coords(p, tp, t, ci, co);
+            spg_tma_store5(&tmap_out, co, base + (uint32_t)s * sb + in_bytes);
+            spg_bulk_commit();
+        }
+    }
+    if (failed) {
+        if (tid == 0) spg_bulk_wait0();     // stores already issued finish reading
+        if (tid == 0 && tp.status) {
+            *(volatile int *)tp.status = 1;
+            // bounded wait for this CTA's own loads still in flight
+            for (int q = 0; q < S; ++q) {
+                const uint32_t mb = mbar0 + 8u * (uint32_t)q;
+                for (uint32_t i = 0; i < 1024u && !spg_mbar_try_wait(mb, 0u) && !spg_mbar_try_wait(mb, 1u); ++i) {
+                }
+            }
+        }
+        return;
+    }
+    if (tid == 0) spg_bulk_wait0();         // stores complete before the CTA retires
+}

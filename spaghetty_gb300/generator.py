@@ -25,7 +25,11 @@ FLAT_VEC = (1, 2)
 HEADER = """// GENERATED by spaghetty_gb300/generator.py -- do not edit.
 // Variant table for arithmetic case {opname}.
 #include "kernels.cuh"
+#include "tma.cuh"
 """
+TMA_THREADS = (128, 256)
+TMA_EPTS = (8, 16)
+TMA_STAGES = (2, 3, 4)
 
 
 STAGES = (2, 3)
@@ -46,6 +50,11 @@ def variants(op: int):
             out.append(("KIND_DIRECT", nt, ept, 0, "spg_direct<%d, %d, %s>" % (nt, ept, OPS[op])))
     for vec in FLAT_VEC:
         out.append(("KIND_FLAT", 256, vec, 0, "spg_flat<%s, %d>" % (OPS[op], vec)))
+    for nt in TMA_THREADS:
+        for ept in TMA_EPTS:
+            for st in TMA_STAGES:
+                out.append(("KIND_TMA", nt, ept, st,
+                            "spg_tiled_tma<%d, %d, %s, %d>" % (nt, ept, OPS[op], st)))
     return out
 
 

@@ -67,7 +67,8 @@ def verify(dims, perm, op=0, sms=152):
 ])
 def test_folding(dims, perm, rank, kind):
     p = plan(dims, perm)
-    assert p["rank"] == rank and p["kind"] == kind
+    # a tiled plan runs on the TMA-staged kernel when its boxes allow it
+    assert p["rank"] == rank and (p["kind"] == kind or (kind, p["kind"]) == ("tiled", "tma"))
     assert int(np.prod(p["dims"])) == int(np.prod(dims))
 
 
