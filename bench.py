@@ -218,6 +218,7 @@ def run_ours(args, ws, rank, local):
     total_ms = 0.0
     total_bytes = 0
     per_size = {}
+    detail = {}
     dom_ms, dom_bytes, dom_n = 0.0, 0, 0
     for evs in all_evs:
         for (dims, perm, f, acc, e0, e1) in evs:
@@ -229,12 +230,21 @@ def run_ours(args, ws, rank, local):
             a = per_size.setdefault(key, [0.0, 0])
             a[0] += ms
             a[1] += b
-            plan = S.plan(dims, perm)
-            if dims == (100, 100, 100, 100) and plan["kind"] == "tiled":
+            plan = S.plan(dims, perm, 1 if acc else 0)
+            dk = (dims, perm, f, acc)
+            dd = detail.setdefault(dk, [0.0, 0, plan["kind"]])
+            dd[0] += ms
+            dd[1] += b
+            if dims == (100, 100, 100, 100) and plan["kind"] in ("tiled", "tma"):
                 dom_ms += ms
                 dom_bytes += b
                 dom_n += 1
     launches = len(cases) * args.steps
+    if args.detail and rank == 0:
+        with open(args.detail, "w") as fh:
+            for (dims, perm, f, acc), (ms, b, kind) in sorted(detail.items()):
+                fh.write(json.dumps({"dims": dims, "perm": perm, "f": f, "acc": acc, "kind": kind,
+                                     "gbs": round(b / (ms / 1e3) / 1e9, 1)}) + "\n")
     t_rank = total_ms / 1e3
     if ws > 1:
         t = torch.tensor([t_rank], dtype=torch.float64)
@@ -267,7 +277,7 @@ def run_ours(args, ws, rank, local):
         tr = traffic_from_profile()
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": tr,
-                "kernel": "spg_tiled (100^4, 18 tiled perms, sort+sortacc)",
+                "kernel": "tiled/TMA transposes at 100^4 (every perm not folded to a copy), sort+sortacc",
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, burst copy)"}
     breakdown = {k: round(v[1] / (v[0] / 1e3) / 1e9, 1) for k, v in per_size.items()}
     line = {
@@ -535,6 +545,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--detail", default=None, help="write per-case GB/s (JSON lines) here")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()
     ws, rank, local = dist_env()

@@ -30,18 +30,18 @@ __device__ __forceinline__ double spg_dmul_branch(double x, double f) {
 }
 
 // x * f for f = +-2^k: when x is normal and x*f is normal, the product is
-// exact and equals x with k added to its exponent field and f's sign applied
-// -- integer operations only.  Every other input (zero, subnormal, inf,
-// NaN) or result (overflow, underflow) takes the rounded multiply, so the
-// bits always equal __dmul_rn(x, f).
-// The fallback multiply sits behind a warp vote so that it is a real
-// (warp-uniform) branch, taken only by warps that hold an inexact case,
-// rather than a multiply computed for every element and then discarded.
+// exact and equals x with k added to its exponent field and f's sign applied.
+// Exponent and sign live in the high 32-bit word, so this is 32-bit integer
+// work only (64-bit integer arithmetic on the bit pattern occupies GB300's
+// scarce FP64 pipe).  Every other input (zero, subnormal, inf, NaN) or
+// result (overflow, underflow) takes the rounded multiply, behind a warp
+// vote so that it is a real branch, so the bits always equal __dmul_rn(x, f).
 __device__ __forceinline__ double spg_pow2(double x, const SpgFactor &F) {
-    const uint64_t b = (uint64_t)__double_as_longlong(x);
-    const uint32_t e = (uint32_t)(b >> 52) & 0x7FFu;
+    const uint32_t hi = (uint32_t)__double2hiint(x);
+    const int lo = __double2loint(x);
+    const uint32_t e = (hi >> 20) & 0x7FFu;
     const bool exact = e - 1u < 2046u && (uint32_t)((int32_t)e + F.k) - 1u < 2046u;
-    double r = __longlong_as_double((long long)((b + (uint64_t)F.kshift) ^ F.sgn));
+    double r = __hiloint2double((int)((hi + ((uint32_t)F.k << 20)) ^ F.sgn_hi), lo);
     if (__any_sync(__activemask(), !exact)) {
         if (!exact) r = spg_dmul_branch(x, F.f);
     }
@@ -51,9 +51,11 @@ __device__ __forceinline__ double spg_pow2(double x, const SpgFactor &F) {
 // x * -1: the sign bit flipped (exact for every non-NaN x, inf included);
 // NaN takes the multiply.
 __device__ __forceinline__ double spg_neg(double x, const SpgFactor &F) {
-    const uint64_t b = (uint64_t)__double_as_longlong(x);
-    const bool exact = (b & 0x7FFFFFFFFFFFFFFFull) <= 0x7FF0000000000000ull;
-    double r = __longlong_as_double((long long)(b ^ 0x8000000000000000ull));
+    const uint32_t hi = (uint32_t)__double2hiint(x);
+    const int lo = __double2loint(x);
+    const uint32_t mag = hi & 0x7FFFFFFFu;
+    const bool exact = mag < 0x7FF00000u || (mag == 0x7FF00000u && lo == 0);
+    double r = __hiloint2double((int)(hi ^ 0x80000000u), lo);
     if (__any_sync(__activemask(), !exact)) {
         if (!exact) r = spg_dmul_branch(x, F.f);
     }

@@ -117,8 +117,7 @@ SpgFactor spg_make_factor(double f, double g) {
     int k = 0;
     if (factor_class(f, &k) == 2) {
         F.k = k;
-        F.kshift = (int64_t)((uint64_t)(int64_t)k << 52);
-        F.sgn = std::signbit(f) ? 0x8000000000000000ull : 0ull;
+        F.sgn_hi = std::signbit(f) ? 0x80000000u : 0u;
     }
     return F;
 }
@@ -647,9 +646,12 @@ int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out) {
     if (pin != kp.vol || pout != kp.vol) return SPAGHETTY_ERR_NOKERNEL;
     const int64_t tile = (int64_t)kp.vol * 8;
     const int64_t tile_al = (tile + 1023) & ~(int64_t)1023;
+    const bool reads_out = spg_op_class(pl.op) != 0;
+    // stage = input tile, [old-output tile (sortacc)], output tile
     out->tp.in_bytes = (int32_t)tile_al;
-    out->tp.stage_bytes = (int32_t)(2 * tile_al);
-    out->tp.tx_bytes = (int32_t)(tile * (spg_op_class(pl.op) == 0 ? 1 : 2));
+    out->tp.out_off = (int32_t)(tile_al * (reads_out ? 2 : 1));
+    out->tp.stage_bytes = (int32_t)(out->tp.out_off + tile_al);
+    out->tp.tx_bytes = (int32_t)(tile * (reads_out ? 2 : 1));
     (void)stages;
     return SPAGHETTY_OK;
 }

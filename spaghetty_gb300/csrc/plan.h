@@ -61,10 +61,8 @@ struct BoxGrid {
 // that is exact (kshift = k << 52, sgn = sign bit of f); see spg_pow2.
 struct SpgFactor {
     double f, g;
-    int64_t kshift;
-    uint64_t sgn;
-    int32_t k;
-    int32_t pad_;
+    int32_t k;          // f = +-2^k
+    uint32_t sgn_hi;    // sign bit of f in the high 32-bit word
 };
 
 struct KParams {
@@ -93,10 +91,10 @@ struct TmaParams {
     int8_t out_mdim[SPG_MAXR];
     int32_t in_mul[SPG_MAXR];
     int32_t out_mul[SPG_MAXR];
-    int32_t stage_bytes;          // input tile + output tile (1024-aligned each)
-    int32_t in_bytes;             // offset of the output tile within a stage
+    int32_t stage_bytes;          // input tile [+ old-output tile] + output tile
+    int32_t in_bytes;             // one tile, 1024-aligned
+    int32_t out_off;              // offset of the output tile within a stage
     int32_t tx_bytes;             // bytes the loads of one box deliver
-    int32_t pad_;
     int *status;                  // error word (bounded waits that timed out)
 };
 

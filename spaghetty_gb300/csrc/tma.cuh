@@ -11,10 +11,13 @@
 // the factor arithmetic applied; for sortacc the old output box is loaded
 // into the output tile by the same bulk load.
 //
-// Pipeline: S stages, each an input tile, an output tile and an mbarrier.
-// Thread 0 issues the loads S-1 boxes ahead and the stores.  Every wait on an
-// mbarrier is bounded: on timeout the kernel records an error in the status
-// word, waits (bounded) for its own loads in flight, and returns.
+// Pipeline: S stages, each an input tile, (sortacc) an old-output tile, an
+// output tile and an mbarrier.  Thread 0 issues the loads S-1 boxes ahead
+// and the stores; loads never target a tile a store may still be reading,
+// and a stage's output tile is rewritten only after the store issued S boxes
+// earlier has finished reading it.  Every wait on an mbarrier is bounded: on
+// timeout the kernel records an error in the status word, waits (bounded)
+// for its own transfers in flight, and returns.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -65,8 +68,9 @@ __device__ __forceinline__ void spg_tma_store5(const void *tmap, const int32_t *
 __device__ __forceinline__ void spg_bulk_commit() {
     asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
 }
-__device__ __forceinline__ void spg_bulk_wait_read0() {
-    asm volatile("cp.async.bulk.wait_group.read 0;\n" ::: "memory");
+template <int N>
+__device__ __forceinline__ void spg_bulk_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;\n" ::"n"(N) : "memory");
 }
 __device__ __forceinline__ void spg_bulk_wait0() {
     asm volatile("cp.async.bulk.wait_group 0;\n" ::: "memory");
@@ -110,7 +114,8 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     const uint32_t base = (raw + 1023u) & ~1023u;
     unsigned char *smem_raw = smem_raw0 + (base - raw);
     const uint32_t sb = (uint32_t)tp.stage_bytes;
-    const uint32_t in_bytes = (uint32_t)tp.in_bytes;
+    const uint32_t in_bytes = (uint32_t)tp.in_bytes;     // old-output tile offset
+    const uint32_t out_off = (uint32_t)tp.out_off;
     const uint32_t mbar0 = base + (uint32_t)S * sb;
     const uint32_t tid = threadIdx.x;
     const uint32_t G = gridDim.x;
@@ -144,6 +149,7 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
         spg_mbar_expect_tx(mb, tx);
         spg_tma_load5(base + (uint32_t)s * sb, &tmap_in, ci, mb);
         if (spg_reads_out<OP>::value) spg_tma_load5(base + (uint32_t)s * sb + in_bytes, &tmap_out, co, mb);
+        (void)co;
     };
 
     if (tid == 0) {
@@ -159,24 +165,28 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
         const int s = it % S;
         if (tid == 0) {
+            // refill the stage box it-1 used: its input (and old-output)
+            // tiles were consumed before the last barrier, and the store of
+            // box it-1 reads only the output tile
             const uint32_t tn = t + (uint32_t)(S - 1) * G;
-            if (tn < p.ntiles) {
-                spg_bulk_wait_read0();      // the stage's previous store has read its tile
-                issue(tn, (it + S - 1) % S);
-            }
+            if (tn < p.ntiles) issue(tn, (it + S - 1) % S);
         }
         const bool ok = spg_mbar_wait(mbar0 + 8u * (uint32_t)s, (uint32_t)((it / S) & 1));
+        // this stage's output tile was last stored S boxes ago: with at most
+        // S-1 newer stores pending, that one has finished reading it
+        if (tid == 0) spg_bulk_wait_read<S - 1>();
         if (__syncthreads_or(!ok)) {         // every thread leaves together
             failed = true;
             break;
         }
         const double *tin = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb);
-        double *tout = reinterpret_cast<double *>(smem_raw + (size_t)s * sb + in_bytes);
+        const double *told = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb + in_bytes);
+        double *tout = reinterpret_cast<double *>(smem_raw + (size_t)s * sb + out_off);
 #pragma unroll
         for (int k = 0; k < EPT; ++k) {
             if (smr[k] >= 0) {
                 const uint32_t e = tid + k * NT;
-                const double y = spg_reads_out<OP>::value ? tout[e] : 0.0;
+                const double y = spg_reads_out<OP>::value ? told[e] : 0.0;
                 tout[e] = spg_apply<OP>(tin[smr[k]], y, fac);
             }
         }
@@ -185,7 +195,7 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
         if (tid == 0) {
             int32_t ci[5], co[5];
             spg_tma_coords(p, tp, t, ci, co);
-            spg_tma_store5(&tmap_out, co, base + (uint32_t)s * sb + in_bytes);
+            spg_tma_store5(&tmap_out, co, base + (uint32_t)s * sb + out_off);
             spg_bulk_commit();
         }
     }
