@@ -239,6 +239,20 @@ int spaghetty_tune_load(const char *path);
  * invariant divisors).  Returns 0 when they pass.  Needs no GPU. */
 int spaghetty_selftest(void);
 
+/* ---- several sortaccs into one output, fused --------------------------- */
+
+/* For k = 0..nsrc-1 in order: sorted = sorted + factors[k] *
+ * permute_{perms[k]}(unsorted[k]), with each product and each sum rounded
+ * as nsrc consecutive tce_sortacc calls round them (bit-identical), but
+ * reading and writing `sorted` once -- the CCSD(T) triples pattern of nine
+ * sortaccs per t3 tile (branches/spaghetty2/ccsd_t_tce_sort_list.txt).
+ * dims: nsrc*rank source dims, as each tce_sortacc call would pass them;
+ * perms: nsrc*rank, 1-based; every permuted shape must equal the output's.
+ * rank <= 6, nsrc <= 16.  Device pointers; asynchronous on `stream`. */
+int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *unsorted,
+                            const int *dims, const int *perms, const double *factors,
+                            double *sorted, void *stream);
+
 /* ---- batched work lists (one persistent launch for many sorts) -------- */
 
 /* One sort of a batch.  Device pointers on the current device.  perm is

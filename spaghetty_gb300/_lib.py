@@ -95,6 +95,10 @@ PROTOTYPES = {
     "spaghetty_batch_info": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64)]),
     "spaghetty_batch_poison": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "spaghetty_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "spaghetty_sortacc_fused": (ctypes.c_int, [ctypes.c_int, ctypes.c_int,
+                                               ctypes.POINTER(ctypes.c_void_p), c_int_p, c_int_p,
+                                               ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+                                               ctypes.c_void_p]),
     "spaghetty_sort_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "spaghetty_selftest": (ctypes.c_int, []),
     "spaghetty_version": (ctypes.c_char_p, []),

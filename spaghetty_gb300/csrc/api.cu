@@ -37,6 +37,9 @@ namespace {
 
 thread_local int g_last_error = 0;
 
+// Dynamic shared memory one CTA may opt into on sm_100-class GPUs (227 KB).
+const int kMaxSmemPerBlock = 232448;
+
 int record(int rc) {
     g_last_error = rc;
     return rc;
@@ -133,6 +136,7 @@ std::string plan_key(int rank, const int *dims, const int *perm, int op, int sms
 
 int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
                        bool allow_tma, Plan *pl);
+int tma_smem_bytes(const TmaLayout &tl, int stages);
 
 // allow_tma: both tensors 16-byte aligned (the bulk tensor copies' rule)
 int make_plan(int rank, const int *dims, const int *perm, double f, double g, int sms, Plan *pl,
@@ -192,17 +196,24 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         TmaLayout tl;
         if (ok_conflicts && spg_tma_layout(*pl, 3, &tl) == SPAGHETTY_OK) {
             const int vol = pl->kp.vol;
-            if (want_tma) {
-                if (ov.threads * ov.ept < vol) return SPAGHETTY_ERR_CONFIG;
-                pl->threads = ov.threads;
-                pl->ept = ov.ept;
-                pl->stages = ov.stages - 10;
+            int stages = want_tma ? ov.stages - 10 : 3;
+            // the stages must fit one CTA's shared memory
+            while (stages > 2 && tma_smem_bytes(tl, stages) > kMaxSmemPerBlock) --stages;
+            if (tma_smem_bytes(tl, stages) > kMaxSmemPerBlock || (want_tma && stages != ov.stages - 10)) {
+                if (want_tma) return SPAGHETTY_ERR_CONFIG;
             } else {
-                pl->threads = vol <= 1024 ? 128 : 256;
-                pl->ept = vol <= 1024 ? 8 : (vol <= 2048 ? 8 : 16);
-                pl->stages = 3;
+                if (want_tma) {
+                    if (ov.threads * ov.ept < vol) return SPAGHETTY_ERR_CONFIG;
+                    pl->threads = ov.threads;
+                    pl->ept = ov.ept;
+                } else {
+                    pl->threads = vol <= 1024 ? 128 : 256;
+                    pl->ept = vol <= 1024 ? 8 : (vol <= 2048 ? 8 : 16);
+                }
+                pl->stages = stages;
+                pl->kind = KIND_TMA;
+                pl->smem_bytes = tma_smem_bytes(tl, stages);
             }
-            pl->kind = KIND_TMA;
         } else if (want_tma) {
             return SPAGHETTY_ERR_CONFIG;
         }
@@ -848,7 +859,8 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     if (rc) return rc;
     if (tma) {
         TmaLayout tl;
-        if (pl.kind != KIND_TILED || threads * ept < pl.kp.vol || spg_tma_layout(pl, stages - 10, &tl))
+        if (pl.kind != KIND_TILED || threads * ept < pl.kp.vol || spg_tma_layout(pl, stages - 10, &tl) ||
+            tma_smem_bytes(tl, stages - 10) > kMaxSmemPerBlock)
             return SPAGHETTY_ERR_CONFIG;
     }
     TuneOverride ov;

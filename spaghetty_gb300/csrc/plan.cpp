@@ -19,6 +19,8 @@ static FastDiv make_fastdiv(uint32_t d) {
     return f;
 }
 
+FastDiv spg_make_fastdiv(uint32_t d) { return make_fastdiv(d); }
+
 // ---------------------------------------------------------------------------
 // Folding.  perm is 1-based (reference convention, trunk/old_sort.f:44-56).
 int spg_fold(int rank, const int *dims, const int *perm, Folded *out) {

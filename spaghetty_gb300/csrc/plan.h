@@ -153,6 +153,7 @@ struct Plan {
 };
 
 // Host-side planning (plan.cpp).  All return a SPAGHETTY_* status.
+FastDiv spg_make_fastdiv(uint32_t d);
 int spg_fold(int rank, const int *dims, const int *perm, Folded *out);
 int spg_choose_op(double f, double g);
 int spg_plan(const Folded &fo, int op, const int *box_override, int threads_override,

@@ -150,3 +150,35 @@ def plan(dims: Sequence[int], perm: Sequence[int], op: int = 0):
 __all__ = ["tce_sort_2", "tce_sortacc_2", "tce_sort_4", "tce_sortacc_4", "tce_sort_6",
            "tce_sortacc_6", "tce_sort_8", "tce_sortacc_8", "sort", "sortacc", "sort_generic",
            "plan", "permuted_shape", "SpaghettyError"]
+
+
+def sortacc_fused(out, sources, perms, factors, stream=None):
+    """out += sum_k factors[k] * sources[k].permute(perms[k] - 1), added in k
+    order with the rounding of consecutive tce_sortacc calls, reading and
+    writing ``out`` once (spaghetty_sortacc_fused).  CUDA FP64 tensors; each
+    source has its own shape (the dims a tce_sortacc call would pass)."""
+    from ._lib import int_array
+    n = len(sources)
+    if not (len(perms) == n == len(factors)) or n == 0:
+        raise ValueError("sources, perms and factors must have one entry per sortacc")
+    rank = sources[0].dim()
+    dims, pp, ptrs = [], [], []
+    for s, p in zip(sources, perms):
+        if s.dim() != rank or len(p) != rank:
+            raise ValueError("every source must have the output's rank")
+        if s.dtype != torch.float64 or not s.is_contiguous() or not s.is_cuda:
+            raise TypeError("sources must be contiguous CUDA FP64 tensors")
+        if permuted_shape(s.shape, p) != tuple(out.shape):
+            raise ValueError("permuted source shape %s != output shape %s"
+                             % (permuted_shape(s.shape, p), tuple(out.shape)))
+        dims += [int(d) for d in s.shape]
+        pp += [int(v) for v in p]
+        ptrs.append(s.data_ptr())
+    if stream is None:
+        stream = torch.cuda.current_stream(out.device).cuda_stream
+    src_arr = (ctypes.c_void_p * n)(*ptrs)
+    fac = (ctypes.c_double * n)(*[float(f) for f in factors])
+    rc = lib().spaghetty_sortacc_fused(rank, n, src_arr, int_array(dims), int_array(pp), fac,
+                                       ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(int(stream)))
+    check(rc, "sortacc_fused")
+    return out

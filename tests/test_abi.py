@@ -78,8 +78,8 @@ def test_plan_invariants_all_rank4_rank6():
     cases += [((17, 29, 64, 100), p) for p in itertools.permutations((1, 2, 3, 4))]
     cases += [((16,) * 6, p) for p in itertools.permutations(range(1, 7))]
     cases += [((12, 20, 16, 20, 12, 16), p) for p in itertools.permutations(range(1, 7))]
-    for dims, perm in cases:
-        p = plan(dims, perm)
+    for (dims, perm), op in itertools.product(cases, (0, 1)):
+        p = plan(dims, perm, op)
         if p["kind"] == "flat":
             continue
         vol = int(np.prod(p["box"]))
@@ -90,6 +90,8 @@ def test_plan_invariants_all_rank4_rank6():
         assert p["run_in"] >= min(32, total) and p["run_out"] >= min(32, total), (dims, perm, p)
         npartial = sum(1 for b, d in zip(p["box"], p["dims"]) if d % b)
         assert npartial <= 2
+        # every plan's shared memory fits one CTA (227 KB opt-in)
+        assert p["smem_bytes"] <= 232448, (dims, perm, p)
 
 
 def test_launch_index_safety_rank4_all_perms():

@@ -1,0 +1,67 @@
+"""Fused sortaccs (spaghetty_sortacc_fused): the nine CCSD(T) triples
+sortaccs of each group in branches/spaghetty2/ccsd_t_tce_sort_list.txt
+applied to one t3 tile in one kernel, bit-identical to applying them one
+after another (the oracle's sequential old_sortacc_6 chain)."""
+import random
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from spaghetty_gb300.workloads import TRIPLES_SORTACC6
+from tests._util import bits_equal, first_mismatch
+
+pytestmark = pytest.mark.gpu
+torch = pytest.importorskip("torch")
+
+
+def source_shape(out_shape, perm):
+    # permute(x, p) has out.shape[q] = x.shape[p_q - 1]
+    shp = [0] * len(perm)
+    for q, p in enumerate(perm):
+        shp[p - 1] = out_shape[q]
+    return tuple(shp)
+
+
+def run_group(cuda, out_shape, perms, factors, seed, share=False):
+    from spaghetty_gb300 import sortacc_fused
+    n = int(np.prod(out_shape))
+    t3 = O.fixture_values(n, seed)
+    srcs_h = []
+    for k, p in enumerate(perms):
+        if share and k > 0 and source_shape(out_shape, p) == source_shape(out_shape, perms[0]):
+            srcs_h.append(srcs_h[0])
+        else:
+            srcs_h.append(O.fixture_values(n, seed + 100 + k))
+    want = t3.copy()
+    for x, p, f in zip(srcs_h, perms, factors):
+        want = O.np_sort(x, source_shape(out_shape, p), p, f, 1.0, out=want)
+    dsrc = [torch.from_numpy(x).to(cuda).reshape(source_shape(out_shape, p))
+            for x, p in zip(srcs_h, perms)]
+    dout = torch.from_numpy(t3.copy()).to(cuda).reshape(out_shape)
+    sortacc_fused(dout, dsrc, perms, factors)
+    got = dout.cpu().numpy().reshape(-1)
+    assert bits_equal(got, want), (out_shape, first_mismatch(got, want))
+
+
+@pytest.mark.parametrize("group", [0, 1, 2])
+def test_triples_groups(cuda, group):
+    perms = TRIPLES_SORTACC6[group]
+    rnd = random.Random(group)
+    factors = [rnd.choice([1.0, -1.0]) for _ in perms]
+    run_group(cuda, (8, 10, 6, 8, 10, 6), perms, factors, 10 * group)
+    run_group(cuda, (16, 16, 16, 16, 16, 16), perms, factors, 10 * group + 3)
+
+
+def test_general_factors_odd_extents_and_rank4(cuda):
+    rnd = random.Random(7)
+    perms6 = TRIPLES_SORTACC6[1][:5]
+    run_group(cuda, (5, 7, 3, 9, 2, 11), perms6, [rnd.uniform(-2, 2) for _ in perms6], 500)
+    perms4 = [(4, 3, 2, 1), (2, 1, 4, 3), (1, 2, 3, 4), (3, 4, 1, 2)]
+    run_group(cuda, (30, 30, 30, 30), perms4, [0.5, -1.0, 0.3, 1.0], 600)
+    run_group(cuda, (17, 29, 6, 10), [(1, 2, 3, 4), (1, 2, 4, 3)], [0.25, -0.75], 700)
+
+
+def test_shared_source(cuda):
+    perms = [TRIPLES_SORTACC6[0][0]] * 3 + list(TRIPLES_SORTACC6[0][1:4])
+    run_group(cuda, (10, 12, 8, 10, 12, 8), perms, [1.0, -1.0, 0.5, 1.0, 1.0, -1.0], 800, share=True)
