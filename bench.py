@@ -254,18 +254,29 @@ def run_ours(args, ws, rank, local):
         t_max = t_rank
     value = total_bytes * ws / t_max / 1e9
 
-    # e2e: same sweep through the C ABI with pinned host buffers
+    # e2e: same sweep through the C ABI with pinned host buffers (the kernels
+    # read and write them in place); the staged variant for comparison
     e2e = None
     if rank == 0 and not args.no_e2e:
         e2e = run_e2e(args, cases, torch, L, int_array, ctypes)
+        L.spaghetty_set_option(1, 0)
+        staged = run_e2e(args, cases, torch, L, int_array, ctypes)
+        L.spaghetty_set_option(1, 1)
+        e2e["staged_copies_value"] = staged["value"]
 
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(args.cpu_seconds)
 
+    secondary = None
+    if not args.no_secondary and rank == 0:
+        del bufs
+        torch.cuda.empty_cache()
+        secondary = {"sort6": run_sort6(args, dev), "triples_fused": run_fused(args, dev),
+                     "autograd": run_autograd(args, dev)}
+        torch.cuda.empty_cache()
     batched = None
     if not args.no_batched:
-        del bufs
         torch.cuda.empty_cache()
         batched = {"config": run_batched(args, dev),
                    "small_tiles": run_batched(args, dev, ext4=(4, 12), ext6=(3, 6))}
@@ -296,6 +307,7 @@ def run_ours(args, ws, rank, local):
         "e2e": e2e,
         "cpu_baseline": cpu,
         "batched": batched,
+        "secondary": secondary,
         "clocks": clocks,
         "wall_s_timed_region": round(wall, 3),
     }
@@ -341,7 +353,8 @@ def run_e2e(args, cases, torch, L, int_array, ctypes):
     return {"value": round(total_b / dt / 1e9, 2), "unit": UNIT,
             "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h // steps,
             "steps": steps, "how": "tce_sort_4/tce_sortacc_4 C-ABI calls on pinned host "
-                                  "buffers, wall clock per sweep"}
+                                  "buffers (read and written in place by the kernels over "
+                                  "NVLink-C2C), wall clock per sweep"}
 
 
 # ---------------------------------------------------------------------------
@@ -498,6 +511,121 @@ def run_batched(args, dev, ext4=(8, 40), ext6=(6, 20), n=4096, seed=2024):
     return out
 
 
+def _timed_events(fn, reps, stream):
+    import torch
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / reps
+
+
+def run_sort6(args, dev):
+    """tce_sort_6 sweep sample: all 720 perms at 10^6, the 54 CCSD(T) perms at
+    16^6 and 20^6, and 48 seeded perms at (12,20,16,20,12,16); sort and
+    sortacc (f = -0.5 / 1.0).  Per-size effective GB/s (L2 flushed before
+    every launch of tensors under 2x L2)."""
+    import random
+    import torch
+    import spaghetty_gb300 as S
+    from spaghetty_gb300.workloads import PERMS6, TRIPLES_SORT6
+    rnd = random.Random(6)
+    groups = [((10,) * 6, PERMS6), ((16,) * 6, TRIPLES_SORT6), ((20,) * 6, TRIPLES_SORT6),
+              ((12, 20, 16, 20, 12, 16), rnd.sample(PERMS6, 48))]
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream(dev)
+    out = {}
+    for dims, perms in groups:
+        n = 1
+        for d in dims:
+            n *= d
+        u = torch.rand(n, dtype=torch.float64, device=dev) - 0.5
+        y = torch.rand(n, dtype=torch.float64, device=dev) - 0.5
+        tot_b = 0
+        tot_t = 0.0
+        for perm in perms:
+            for acc in (False, True):
+                if n * 16 < 2 * L2_BYTES:
+                    flush.fill_(1.0)
+                t = _timed_events(lambda: S.sort_generic(u, y, dims, perm, 1.0 if acc else -0.5,
+                                                         1.0 if acc else 0.0), 1, stream)
+                tot_t += t
+                tot_b += n * (24 if acc else 16)
+        out["x".join(map(str, dims))] = {"gbs": round(tot_b / tot_t / 1e9, 1), "launches": 2 * len(perms)}
+        del u, y
+    return out
+
+
+def run_fused(args, dev):
+    """The nine triples sortaccs of each group applied to one t3 tile: fused
+    (one kernel, t3 read and written once) against nine sortacc launches.
+    GB/s counts each path's own algorithmic bytes; speedup is in time."""
+    import torch
+    import spaghetty_gb300 as S
+    from spaghetty_gb300.workloads import TRIPLES_SORTACC6
+    stream = torch.cuda.current_stream(dev)
+    res = {}
+    for ext in (16, 20):
+        shape = (ext,) * 6
+        n = ext ** 6
+        t3 = torch.rand(shape, dtype=torch.float64, device=dev) - 0.5
+        srcs = [torch.rand(shape, dtype=torch.float64, device=dev) - 0.5 for _ in range(9)]
+        rows = []
+        for gi, perms in enumerate(TRIPLES_SORTACC6):
+            facs = [1.0 if k % 3 else -1.0 for k in range(9)]
+
+            def fused():
+                S.sortacc_fused(t3, srcs, perms, facs)
+
+            def seq():
+                for x, p, f in zip(srcs, perms, facs):
+                    S.sort_generic(x, t3, shape, p, f, 1.0)
+
+            for _ in range(2):
+                fused()
+                seq()
+            tf = _timed_events(fused, 3, stream)
+            ts = _timed_events(seq, 3, stream)
+            rows.append({"group": gi, "fused_ms": round(tf * 1e3, 3), "seq_ms": round(ts * 1e3, 3),
+                         "fused_gbs": round((16 * n + 8 * n * 9) / tf / 1e9, 1),
+                         "seq_gbs": round(9 * 24 * n / ts / 1e9, 1),
+                         "speedup": round(ts / tf, 2)})
+        res["%d^6" % ext] = rows
+        del t3, srcs
+    return res
+
+
+def run_autograd(args, dev):
+    """y = sum_k f_k * permute_k(x) over 3 seeded perms and its hand-written
+    backward, forward+backward GB/s (each pass: one sort + two sortaccs)."""
+    import torch
+    from spaghetty_gb300.autograd import permute_sum
+    stream = torch.cuda.current_stream(dev)
+    res = {}
+    for dims, perms in [((24,) * 4, [(4, 3, 2, 1), (2, 4, 1, 3), (3, 1, 4, 2)]),
+                        ((12,) * 6, [(6, 5, 4, 3, 2, 1), (2, 6, 1, 5, 4, 3), (4, 3, 6, 2, 1, 5)])]:
+        n = 1
+        for d in dims:
+            n *= d
+        x = (torch.rand(dims, dtype=torch.float64, device=dev) - 0.5).requires_grad_(True)
+        g = torch.rand(dims, dtype=torch.float64, device=dev)
+
+        def step():
+            x.grad = None
+            y = permute_sum(x, perms, (0.75, -1.25, 0.3))
+            y.backward(g)
+
+        for _ in range(3):
+            step()
+        t = _timed_events(step, 10, stream)
+        res["x".join(map(str, dims))] = {"fwd_bwd_gbs": round(2 * (16 + 2 * 24) * n / t / 1e9, 1),
+                                          "ms": round(t * 1e3, 4)}
+    return res
+
+
 def run_case(args):
     """One sort case, W warm-up + K timed launches (the profiling workload)."""
     import torch
@@ -545,6 +673,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--detail", default=None, help="write per-case GB/s (JSON lines) here")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     args = ap.parse_args()

@@ -170,6 +170,14 @@ int spaghetty_sort(int rank, const double *unsorted, double *sorted,
 int spaghetty_last_error(void);
 const char *spaghetty_error_string(int code);
 
+/* Library options.  SPAGHETTY_OPT_HOST_ZERO_COPY (default 1): the
+ * synchronous entry points run the kernels directly on PINNED host buffers
+ * through their mapped device addresses (over NVLink-C2C on GB300) instead
+ * of staging them through device copies; 0 stages every host buffer.
+ * Pageable host buffers are always staged. */
+#define SPAGHETTY_OPT_HOST_ZERO_COPY 1
+int spaghetty_set_option(int option, int value);
+
 /* Synchronise the current device and report (then clear) the kernels'
  * status word: SPAGHETTY_ERR_DEVICE if a kernel gave up a bounded wait (its
  * pipeline's transfers did not arrive in time), else SPAGHETTY_OK.  The

@@ -78,6 +78,7 @@ PROTOTYPES = {
                                       c_int_p, c_int_p, ctypes.c_double, ctypes.c_double]),
     "spaghetty_last_error": (ctypes.c_int, []),
     "spaghetty_device_status": (ctypes.c_int, []),
+    "spaghetty_set_option": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "spaghetty_error_string": (ctypes.c_char_p, [ctypes.c_int]),
     "spaghetty_plan_query": (ctypes.c_int, [ctypes.c_int, c_int_p, c_int_p, ctypes.c_int,
                                             ctypes.POINTER(PlanInfo)]),

@@ -361,9 +361,17 @@ bool overlaps(const double *a, const double *b, int64_t n) {
     return a0 < b1 && b0 < a1;
 }
 
-// Where a pointer lives.  0 = host memory (pageable or pinned), 1 = memory a
-// kernel on `dev` may access (device or managed).
-int classify(const void *p, int *dev) {
+// Host buffers that are pinned (page-locked, registered with CUDA) are read
+// and written by the kernels in place through their mapped device address --
+// over NVLink-C2C on GB300, both directions at once -- instead of being
+// staged with copies.  spaghetty_set_option(SPAGHETTY_OPT_HOST_ZERO_COPY, 0)
+// turns that off (staging for every host buffer).
+int g_zero_copy = 1;
+
+// Where a pointer lives.  0 = pageable host memory, 1 = memory a kernel on
+// `dev` may access (device or managed), 2 = pinned host memory (its mapped
+// device address in *mapped).
+int classify(const void *p, int *dev, const void **mapped) {
     cudaPointerAttributes at;
     std::memset(&at, 0, sizeof(at));
     cudaError_t e = cudaPointerGetAttributes(&at, p);
@@ -373,7 +381,12 @@ int classify(const void *p, int *dev) {
     }
     if (at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged) {
         *dev = at.device;
+        if (mapped) *mapped = p;
         return 1;
+    }
+    if (at.type == cudaMemoryTypeHost && at.devicePointer && g_zero_copy) {
+        if (mapped) *mapped = at.devicePointer;
+        return 2;
     }
     return 0;
 }
@@ -421,7 +434,8 @@ int sort_sync(int rank, const double *u, double *s, const int *dims, const int *
     if (!u || !s) return SPAGHETTY_ERR_NULL;
     if (overlaps(u, s, fo.nelem)) return SPAGHETTY_ERR_ALIAS;
     int du = -1, ds = -1;
-    const int ku = classify(u, &du), ks = classify(s, &ds);
+    const void *mu = nullptr, *ms = nullptr;
+    int ku = classify(u, &du, &mu), ks = classify(s, &ds, &ms);
     if (ku < 0 || ks < 0) return SPAGHETTY_ERR_CUDA;
     int dev = ku == 1 ? du : (ks == 1 ? ds : -1);
     if (ku == 1 && ks == 1 && du != ds) return SPAGHETTY_ERR_MEMSPACE;
@@ -429,23 +443,25 @@ int sort_sync(int rank, const double *u, double *s, const int *dims, const int *
     if (dev < 0 && cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
     Plan pl;
     // staged sides use cudaMalloc'd buffers (aligned); device sides are the
-    // caller's pointers
-    const bool allow_tma = (ku == 1 ? aligned16(u) : true) && (ks == 1 ? aligned16(s) : true);
+    // caller's pointers; pinned host sides are used in place, where the bulk
+    // tensor copies are not used
+    const bool allow_tma = ku != 2 && ks != 2 && (ku == 1 ? aligned16(u) : true) &&
+                           (ks == 1 ? aligned16(s) : true);
     rc = make_plan(rank, dims, perm, f, g, device_sms(dev), &pl, allow_tma);
     if (rc) return rc;
     cudaStream_t st = 0;  // legacy default stream: ordered after prior blocking-stream work
     const size_t n = (size_t)fo.nelem;
     const size_t bytes = n * sizeof(double);
-    if (ku == 1 && ks == 1) {
-        rc = launch_plan(pl, u, s, st, dev);
+    if (ku != 0 && ks != 0) {
+        rc = launch_plan(pl, (const double *)mu, (double *)ms, st, dev);
         if (rc) return rc;
         if (cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
         return take_device_status();
     }
     std::lock_guard<std::mutex> lk(g_stage_mu);
     Staging &sg = g_stage[dev];
-    const double *du_ptr = u;
-    double *ds_ptr = s;
+    const double *du_ptr = ku == 2 ? (const double *)mu : u;
+    double *ds_ptr = ks == 2 ? (double *)ms : s;
     if (ku == 0) {
         if ((rc = grow(&sg.u, &sg.nu, n))) return rc;
         if (cudaMemcpyAsync(sg.u, u, bytes, cudaMemcpyHostToDevice, st) != cudaSuccess) goto cuda_fail;
@@ -594,6 +610,14 @@ const char *spaghetty_error_string(int code) {
 }
 
 int spaghetty_last_error(void) { return g_last_error; }
+
+int spaghetty_set_option(int option, int value) {
+    if (option == SPAGHETTY_OPT_HOST_ZERO_COPY) {
+        g_zero_copy = value ? 1 : 0;
+        return SPAGHETTY_OK;
+    }
+    return SPAGHETTY_ERR_CONFIG;
+}
 
 int spaghetty_device_status(void) {
     if (cudaDeviceSynchronize() != cudaSuccess) {

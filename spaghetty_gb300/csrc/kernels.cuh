@@ -21,12 +21,12 @@
 #include <stdint.h>
 #include "plan.h"
 
-// Rounded FP64 multiply as volatile PTX: it cannot be hoisted out of the
-// rarely taken branches below and computed for every element.
-__device__ __forceinline__ double spg_dmul_branch(double x, double f) {
-    double r;
-    asm volatile("mul.rn.f64 %0, %1, %2;\n" : "=d"(r) : "d"(x), "d"(f));
-    return r;
+// The rounded FP64 multiply of the rarely taken inexact cases, kept out of
+// line: inlined, the compiler predicates it (or hoists it) into the common
+// path, where a predicated-off FP64 instruction still occupies GB300's
+// narrow FP64 pipe for every element.
+static __device__ __noinline__ double spg_dmul_branch(double x, double f) {
+    return __dmul_rn(x, f);
 }
 
 // x * f for f = +-2^k: when x is normal and x*f is normal, the product is

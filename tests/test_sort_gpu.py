@@ -253,11 +253,22 @@ def test_host_buffers_are_staged(cuda):
         ps = torch.from_numpy(y).pin_memory()
         call_dropin("tce_sortacc_4", pu.data_ptr(), ps.data_ptr(), dims, perm, 0.5)
         check(ps.numpy(), O.np_sort(u, dims, perm, 0.5, 1.0, out=y), ("pinned", perm))
-        # mixed: device input, host output
+        # pinned buffers staged through device copies instead of used in place
+        assert lib().spaghetty_set_option(1, 0) == 0
+        try:
+            ps = torch.from_numpy(y).pin_memory()
+            call_dropin("tce_sortacc_4", pu.data_ptr(), ps.data_ptr(), dims, perm, -1.0)
+            check(ps.numpy(), O.np_sort(u, dims, perm, -1.0, 1.0, out=y), ("pinned staged", perm))
+        finally:
+            lib().spaghetty_set_option(1, 1)
+        # mixed: device input, host output (pageable and pinned)
         du = dev(u, cuda)
         s = np.zeros(n)
         call_dropin("tce_sort_4", du.data_ptr(), s.ctypes.data, dims, perm, 1.0)
         check(s, O.np_sort(u, dims, perm, 1.0), ("mixed", perm))
+        ps = torch.zeros(n, dtype=torch.float64).pin_memory()
+        call_dropin("tce_sort_4", du.data_ptr(), ps.data_ptr(), dims, perm, 0.5)
+        check(ps.numpy(), O.np_sort(u, dims, perm, 0.5), ("mixed pinned", perm))
 
 
 def test_async_on_side_stream(cuda):
