@@ -136,8 +136,8 @@ def case_bytes(dims, acc):
 
 def traffic_from_profile():
     """dram bytes per launch of the dominant kernel, from the committed ncu
-    summary (profiles/tiled_sort4_100.md, line 'traffic_bytes_per_launch: X')."""
-    path = os.path.join(ROOT, "profiles", "tiled_sort4_100.md")
+    summary (profiles/tma_sort4_100.md, line 'traffic_bytes_per_launch: X')."""
+    path = os.path.join(ROOT, "profiles", "tma_sort4_100.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch:"):
@@ -235,7 +235,7 @@ def run_ours(args, ws, rank, local):
             dd = detail.setdefault(dk, [0.0, 0, plan["kind"]])
             dd[0] += ms
             dd[1] += b
-            if dims == (100, 100, 100, 100) and plan["kind"] in ("tiled", "tma"):
+            if dims == (100, 100, 100, 100) and plan["kind"] == "tma" and not acc:
                 dom_ms += ms
                 dom_bytes += b
                 dom_n += 1
@@ -288,7 +288,9 @@ def run_ours(args, ws, rank, local):
         tr = traffic_from_profile()
         roof = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": tr,
-                "kernel": "tiled/TMA transposes at 100^4 (every perm not folded to a copy), sort+sortacc",
+                "kernel": "spg_tiled_tma, sort (16 B/element), 100^4: every perm planned on the "
+                          "TMA-staged kernel, factors 1, -1, 0.5",
+                "launches": dom_n,
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, burst copy)"}
     breakdown = {k: round(v[1] / (v[0] / 1e3) / 1e9, 1) for k, v in per_size.items()}
     line = {
@@ -358,18 +360,20 @@ def run_e2e(args, cases, torch, L, int_array, ctypes):
 
 
 # ---------------------------------------------------------------------------
-def cpu_sweep_sample(budget_s: float, threads: int | None = None):
-    """The reference's C loop nests on the host cores: tune the loop order at
-    30^4 (all 24 per permutation, the reference's brute-force method), then
-    time a bounded sample of the sweep.  Returns (GB/s, cores, description)."""
+_CPU_STATE = {}
+
+
+def _cpu_setup():
+    """Build/load the reference nests, tune the loop order of every perm at
+    30^4 (all 24 orders, the reference's brute-force method,
+    trunk/generator2.py:581-598) once, and make the sweep's buffers."""
     import numpy as np
     from oracle import refnests as R
     from spaghetty_gb300.workloads import PERMS4, SORT4_DIMS
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
+    if _CPU_STATE:
+        return _CPU_STATE
     if R.load() is None:
         return None
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     tdims = (30, 30, 30, 30)
     n = 30 ** 4
     rng = np.random.default_rng(3)
@@ -390,23 +394,43 @@ def cpu_sweep_sample(budget_s: float, threads: int | None = None):
     for dims in SORT4_DIMS:
         m = int(np.prod(dims))
         bufs[dims] = (rng.uniform(-1, 1, m), rng.uniform(-1, 1, m))
+    _CPU_STATE.update(best=best, bufs=bufs, R=R)
+    return _CPU_STATE
+
+
+def cpu_sweep_sample(budget_s: float, threads: int | None = None, start: int = 0):
+    """The reference's C loop nests on the host cores (best loop order per
+    perm, tuned once at 30^4), timed over a bounded sample of the sweep
+    starting at case `start`.  Returns (GB/s, cores, description, next)."""
+    from spaghetty_gb300.workloads import PERMS4, SORT4_DIMS, SORT4_FACTORS
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    st = _cpu_setup()
+    if st is None:
+        return None
+    R, best, bufs = st["R"], st["best"], st["bufs"]
+    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
     total_b, total_t, calls = 0, 0.0, 0
-    order = [(d, p, acc) for d in SORT4_DIMS for p in PERMS4 for acc in (False, True)]
+    # sizes interleaved, so that any bounded prefix weights the sizes as the
+    # whole sweep does
+    order = [(d, p, f, acc) for p in PERMS4 for f in SORT4_FACTORS for acc in (False, True)
+             for d in SORT4_DIMS]
     t_start = time.perf_counter()
-    for (dims, perm, acc) in order:
-        if time.perf_counter() - t_start > budget_s:
-            break
+    i = start
+    while calls < len(order) and time.perf_counter() - t_start <= budget_s:
+        dims, perm, f, acc = order[i % len(order)]
         uu, ss = bufs[dims]
         t0 = time.perf_counter()
-        R.call(perm, best[perm], uu, ss, dims, 0.5, 1.0 if acc else 0.0)
+        R.call(perm, best[perm], uu, ss, dims, f, 1.0 if acc else 0.0)
         total_t += time.perf_counter() - t0
         total_b += case_bytes(dims, acc)
         calls += 1
-    desc = ("reference generated C nests (trunk/generator2.py emitter, OpenMP, gcc -O3 "
-            "-ffp-contract=off), best of 24 loop orders per perm tuned at 30^4; %d calls of the "
-            "sweep (sizes in order 20^4..100^4, 17x29x64x100; f=0.5; sort+sortacc) within %.0f s"
-            % (calls, budget_s))
-    return total_b / total_t / 1e9, cores, desc
+        i += 1
+    desc = ("reference generated C nests (trunk/generator2.py emitter, OpenMP over %d host "
+            "threads, gcc -O3 -ffp-contract=off), best of 24 loop orders per perm tuned at 30^4; "
+            "%d calls of the sweep (24 perms x 5 sizes x f{1,-1,0.5} x sort/sortacc, the five "
+            "sizes interleaved, from case %d) within a %.0f s budget" % (cores, calls, start % len(order), budget_s))
+    return total_b / total_t / 1e9, cores, desc, i
 
 
 def cpu_baseline(budget_s):
@@ -416,7 +440,7 @@ def cpu_baseline(budget_s):
         return {"value": None, "unit": UNIT, "error": str(e)[:200]}
     if r is None:
         return {"value": None, "unit": UNIT, "error": "reference nests unavailable"}
-    v, cores, desc = r
+    v, cores, desc, _ = r
     return {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": "reference",
             "sample": desc}
 
@@ -428,13 +452,14 @@ def run_reference(args, ws, rank):
     if R.load() is None:
         return {"impl": "reference", "unavailable": "reference C nests could not be built here"}
     per_step = max(2.0, min(12.0, 150.0 / max(1, args.steps + args.warmup)))
+    nxt = 0
     for _ in range(args.warmup):
-        cpu_sweep_sample(per_step)
+        _, _, _, nxt = cpu_sweep_sample(per_step, start=nxt)
     vals = []
     t0 = time.perf_counter()
     cores, desc = None, None
     for _ in range(args.steps):
-        v, cores, desc = cpu_sweep_sample(per_step)
+        v, cores, desc, nxt = cpu_sweep_sample(per_step, start=nxt)
         vals.append(v)
     wall = time.perf_counter() - t0
     value = statistics.median(vals)

@@ -164,6 +164,21 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
     return rc;
 }
 
+// Switch a built tiled plan to the TMA-staged kernel with the given shape.
+int to_tma(Plan *pl, int threads, int ept, int stages, bool strict) {
+    TmaLayout tl;
+    if (pl->kind != KIND_TILED || threads * ept < pl->kp.vol ||
+        spg_tma_layout(*pl, stages, &tl) != SPAGHETTY_OK ||
+        tma_smem_bytes(tl, stages) > kMaxSmemPerBlock)
+        return strict ? SPAGHETTY_ERR_CONFIG : SPAGHETTY_ERR_NOKERNEL;
+    pl->threads = threads;
+    pl->ept = ept;
+    pl->stages = stages;
+    pl->kind = KIND_TMA;
+    pl->smem_bytes = tma_smem_bytes(tl, stages);
+    return SPAGHETTY_OK;
+}
+
 int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
                        bool allow_tma, Plan *pl) {
     Folded fo;
@@ -178,44 +193,38 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         if (it != g_tune.end()) { ov = it->second; have = true; }
     }
     // an override with stages 12..14 asks for the TMA kernel (2..4 stages);
-    // the tiled plan underneath is built with the async kernel's shape
+    // it is ignored where the TMA kernel cannot run (misaligned or host
+    // buffers), which then get the default plan
+    if (have && ov.stages >= 12 && !allow_tma) have = false;
     const bool want_tma = have && ov.stages >= 12;
     if (have) {
         rc = want_tma ? spg_plan(fo, op, ov.box, 256, 16, 0, sms, pl)
                       : spg_plan(fo, op, ov.box, ov.threads, ov.ept, ov.stages, sms, pl);
-    } else {
-        rc = spg_plan(fo, op, nullptr, 0, 0, 0, sms, pl);
+        if (rc) return rc;
+        rc = spg_build_params(pl, f, g);
+        if (rc) return rc;
+        if (want_tma) return to_tma(pl, ov.threads, ov.ept, ov.stages - 10, true);
+        return SPAGHETTY_OK;
     }
+    rc = spg_plan(fo, op, nullptr, 0, 0, 0, sms, pl);
     if (rc) return rc;
     rc = spg_build_params(pl, f, g);
     if (rc) return rc;
-    if (pl->kind == KIND_TILED && allow_tma && (!have || want_tma)) {
-        // default: the TMA kernel when its unpadded tile reads at most 2-way
-        // bank conflicts in the permute step
-        const bool ok_conflicts = want_tma || pl->wf_pad0 <= 2 * pl->wf_ideal;
-        TmaLayout tl;
-        if (ok_conflicts && spg_tma_layout(*pl, 3, &tl) == SPAGHETTY_OK) {
-            const int vol = pl->kp.vol;
-            int stages = want_tma ? ov.stages - 10 : 3;
-            // the stages must fit one CTA's shared memory
-            while (stages > 2 && tma_smem_bytes(tl, stages) > kMaxSmemPerBlock) --stages;
-            if (tma_smem_bytes(tl, stages) > kMaxSmemPerBlock || (want_tma && stages != ov.stages - 10)) {
-                if (want_tma) return SPAGHETTY_ERR_CONFIG;
-            } else {
-                if (want_tma) {
-                    if (ov.threads * ov.ept < vol) return SPAGHETTY_ERR_CONFIG;
-                    pl->threads = ov.threads;
-                    pl->ept = ov.ept;
-                } else {
-                    pl->threads = vol <= 1024 ? 128 : 256;
-                    pl->ept = vol <= 1024 ? 8 : (vol <= 2048 ? 8 : 16);
-                }
-                pl->stages = stages;
-                pl->kind = KIND_TMA;
-                pl->smem_bytes = tma_smem_bytes(tl, stages);
+    if (pl->kind == KIND_TILED && allow_tma) {
+        // default TMA plan: its own (smaller) box, 256 threads, 3 stages
+        // when three CTAs fit an SM, else 2; kept only when its unpadded
+        // tile reads at most 2-way bank conflicts in the permute step
+        int box[SPG_MAXR];
+        Plan tp;
+        if (spg_default_box_tma(fo, sms, box) == SPAGHETTY_OK &&
+            spg_plan(fo, op, box, 256, 8, 0, sms, &tp) == SPAGHETTY_OK &&
+            spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_TILED &&
+            tp.wf_pad0 <= 2 * tp.wf_ideal) {
+            TmaLayout tl;
+            if (spg_tma_layout(tp, 3, &tl) == SPAGHETTY_OK) {
+                const int stages = tma_smem_bytes(tl, 3) * 3 <= 228 * 1024 ? 3 : 2;
+                if (to_tma(&tp, 256, 8, stages, false) == SPAGHETTY_OK) *pl = tp;
             }
-        } else if (want_tma) {
-            return SPAGHETTY_ERR_CONFIG;
         }
     }
     return SPAGHETTY_OK;
