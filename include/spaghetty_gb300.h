@@ -122,6 +122,47 @@ void tce_sortacc_8_(const double *unsorted, double *sorted,
                     const int *m, const int *n, const int *o, const int *p,
                     const double *factor);
 
+/* -i8 shims for NWChem built with 8-byte default integers: the same
+ * drop-ins with dims and permutation as int64 (values must fit 32 bits).
+ * Link them under the plain names with the linker's symbol renaming, or call
+ * them through a Fortran bind(C) interface. */
+void tce_sort_4_i8(const double *unsorted, double *sorted,
+                   const int64_t *a, const int64_t *b, const int64_t *c, const int64_t *d,
+                   const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l,
+                   const double *factor);
+void tce_sort_4_i8_(const double *unsorted, double *sorted,
+                    const int64_t *a, const int64_t *b, const int64_t *c, const int64_t *d,
+                    const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l,
+                    const double *factor);
+void tce_sortacc_4_i8(const double *unsorted, double *sorted,
+                      const int64_t *a, const int64_t *b, const int64_t *c, const int64_t *d,
+                      const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l,
+                      const double *factor);
+void tce_sortacc_4_i8_(const double *unsorted, double *sorted,
+                       const int64_t *a, const int64_t *b, const int64_t *c, const int64_t *d,
+                       const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l,
+                       const double *factor);
+void tce_sort_6_i8(const double *unsorted, double *sorted,
+                   const int64_t *a, const int64_t *b, const int64_t *c, const int64_t *d,
+                   const int64_t *e, const int64_t *f,
+                   const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l,
+                   const int64_t *m, const int64_t *n, const double *factor);
+void tce_sort_6_i8_(const double *unsorted, double *sorted,
+                    const int64_t *a, const int64_t *b, const int64_t *c, const int64_t *d,
+                    const int64_t *e, const int64_t *f,
+                    const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l,
+                    const int64_t *m, const int64_t *n, const double *factor);
+void tce_sortacc_6_i8(const double *unsorted, double *sorted,
+                      const int64_t *a, const int64_t *b, const int64_t *c, const int64_t *d,
+                      const int64_t *e, const int64_t *f,
+                      const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l,
+                      const int64_t *m, const int64_t *n, const double *factor);
+void tce_sortacc_6_i8_(const double *unsorted, double *sorted,
+                       const int64_t *a, const int64_t *b, const int64_t *c, const int64_t *d,
+                       const int64_t *e, const int64_t *f,
+                       const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l,
+                       const int64_t *m, const int64_t *n, const double *factor);
+
 /* Status-returning forms of the rank-4/6 drop-ins: same arguments, return a
  * SPAGHETTY_* code instead of printing (the reference's tce_sort4_switch.F
  * :58-60 can only print 'something is wrong...' and return). */

@@ -60,7 +60,15 @@ _R6 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 12 + [c_double_p]
 _R8 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 16 + [c_double_p]
 _R2 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 4 + [c_double_p]
 
+c_int64_p = ctypes.POINTER(ctypes.c_int64)
+_R4_I8 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int64_p] * 8 + [c_double_p]
+_R6_I8 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int64_p] * 12 + [c_double_p]
+
 PROTOTYPES = {
+    "tce_sort_4_i8": (None, _R4_I8), "tce_sort_4_i8_": (None, _R4_I8),
+    "tce_sortacc_4_i8": (None, _R4_I8), "tce_sortacc_4_i8_": (None, _R4_I8),
+    "tce_sort_6_i8": (None, _R6_I8), "tce_sort_6_i8_": (None, _R6_I8),
+    "tce_sortacc_6_i8": (None, _R6_I8), "tce_sortacc_6_i8_": (None, _R6_I8),
     "tce_sort_2": (None, _R2), "tce_sort_2_": (None, _R2),
     "tce_sortacc_2": (None, _R2), "tce_sortacc_2_": (None, _R2),
     "tce_sort_4": (None, _R4), "tce_sort_4_": (None, _R4),

@@ -967,4 +967,56 @@ void tce_sort_8_(SPG_R8_ARGS) { r8("tce_sort_8", true, unsorted, sorted, a, b, c
 void tce_sortacc_8(SPG_R8_ARGS) { r8("tce_sortacc_8", true, unsorted, sorted, a, b, c, d, e, f, g, h, i, j, k, l, m, n, o, p, factor, 1.0); }
 void tce_sortacc_8_(SPG_R8_ARGS) { r8("tce_sortacc_8", true, unsorted, sorted, a, b, c, d, e, f, g, h, i, j, k, l, m, n, o, p, factor, 1.0); }
 
+// ---- -i8 shims: NWChem built with 8-byte default integers passes dims and
+// permutation as int64 (trunk/generator2.py:926-932 lists the reference's
+// compiler flag tables; the Fortran callers are unchanged).  Values must fit
+// 32 bits; anything larger is rejected as bad dims.
+static bool narrow(const int64_t *const *src, int n, int *dst) {
+    for (int q = 0; q < n; ++q) {
+        if (!src[q]) return false;
+        const int64_t v = *src[q];
+        if (v < INT32_MIN || v > INT32_MAX) return false;
+        dst[q] = (int)v;
+    }
+    return true;
+}
+static int r4_i8(const char *w, bool pr, const double *u, double *s, const int64_t *a, const int64_t *b,
+                 const int64_t *c, const int64_t *d, const int64_t *i, const int64_t *j, const int64_t *k,
+                 const int64_t *l, const double *f, double g) {
+    const int64_t *src[8] = {a, b, c, d, i, j, k, l};
+    int v[8];
+    if (!narrow(src, 8, v)) {
+        record(SPAGHETTY_ERR_DIMS);
+        if (pr) std::fprintf(stderr, "spaghetty_gb300: %s: dims or permutation out of range\n", w);
+        return SPAGHETTY_ERR_DIMS;
+    }
+    return call_r(w, pr, 4, u, s, v, v + 4, *f, g);
+}
+static int r6_i8(const char *w, bool pr, const double *u, double *s, const int64_t *a, const int64_t *b,
+                 const int64_t *c, const int64_t *d, const int64_t *e, const int64_t *ff, const int64_t *i,
+                 const int64_t *j, const int64_t *k, const int64_t *l, const int64_t *m, const int64_t *n,
+                 const double *f, double g) {
+    const int64_t *src[12] = {a, b, c, d, e, ff, i, j, k, l, m, n};
+    int v[12];
+    if (!narrow(src, 12, v)) {
+        record(SPAGHETTY_ERR_DIMS);
+        if (pr) std::fprintf(stderr, "spaghetty_gb300: %s: dims or permutation out of range\n", w);
+        return SPAGHETTY_ERR_DIMS;
+    }
+    return call_r(w, pr, 6, u, s, v, v + 6, *f, g);
+}
+#define SPG_I8_R4 const double *u, double *s, const int64_t *a, const int64_t *b, const int64_t *c, \
+    const int64_t *d, const int64_t *i, const int64_t *j, const int64_t *k, const int64_t *l, const double *f
+#define SPG_I8_R6 const double *u, double *s, const int64_t *a, const int64_t *b, const int64_t *c, \
+    const int64_t *d, const int64_t *e, const int64_t *ff, const int64_t *i, const int64_t *j, \
+    const int64_t *k, const int64_t *l, const int64_t *m, const int64_t *n, const double *f
+void tce_sort_4_i8(SPG_I8_R4) { r4_i8("tce_sort_4", true, u, s, a, b, c, d, i, j, k, l, f, 0.0); }
+void tce_sort_4_i8_(SPG_I8_R4) { r4_i8("tce_sort_4", true, u, s, a, b, c, d, i, j, k, l, f, 0.0); }
+void tce_sortacc_4_i8(SPG_I8_R4) { r4_i8("tce_sortacc_4", true, u, s, a, b, c, d, i, j, k, l, f, 1.0); }
+void tce_sortacc_4_i8_(SPG_I8_R4) { r4_i8("tce_sortacc_4", true, u, s, a, b, c, d, i, j, k, l, f, 1.0); }
+void tce_sort_6_i8(SPG_I8_R6) { r6_i8("tce_sort_6", true, u, s, a, b, c, d, e, ff, i, j, k, l, m, n, f, 0.0); }
+void tce_sort_6_i8_(SPG_I8_R6) { r6_i8("tce_sort_6", true, u, s, a, b, c, d, e, ff, i, j, k, l, m, n, f, 0.0); }
+void tce_sortacc_6_i8(SPG_I8_R6) { r6_i8("tce_sortacc_6", true, u, s, a, b, c, d, e, ff, i, j, k, l, m, n, f, 1.0); }
+void tce_sortacc_6_i8_(SPG_I8_R6) { r6_i8("tce_sortacc_6", true, u, s, a, b, c, d, e, ff, i, j, k, l, m, n, f, 1.0); }
+
 }  // extern "C"

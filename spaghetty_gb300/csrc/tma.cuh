@@ -121,6 +121,28 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     const uint32_t G = gridDim.x;
     const uint32_t tx = (uint32_t)tp.tx_bytes;
 
+    auto issue = [&](uint32_t t, int s) {
+        int32_t ci[5], co[5];
+        spg_tma_coords(p, tp, t, ci, co);
+        const uint32_t mb = mbar0 + 8u * (uint32_t)s;
+        spg_mbar_expect_tx(mb, tx);
+        spg_tma_load5(base + (uint32_t)s * sb, &tmap_in, ci, mb);
+        if (spg_reads_out<OP>::value) spg_tma_load5(base + (uint32_t)s * sb + in_bytes, &tmap_out, co, mb);
+        (void)co;
+    };
+
+    // thread 0 sets up the barriers and puts the first S-1 boxes in flight
+    // before anyone builds tables, so DRAM latency overlaps the prologue
+    if (tid == 0) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) spg_mbar_init(mbar0 + 8u * s, 1u);
+        spg_fence_mbar_init();
+#pragma unroll
+        for (int q = 0; q < S - 1; ++q) {
+            const uint32_t t = blockIdx.x + (uint32_t)q * G;
+            if (t < p.ntiles) issue(t, q);
+        }
+    }
     // element tables: output-tile element e = tid + k*NT takes input-tile
     // element smr[k]
     int32_t smr[EPT];
@@ -135,30 +157,7 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
             smr[k] = lin;
         }
     }
-    if (tid == 0) {
-#pragma unroll
-        for (int s = 0; s < S; ++s) spg_mbar_init(mbar0 + 8u * s, 1u);
-        spg_fence_mbar_init();
-    }
-    __syncthreads();
-
-    auto issue = [&](uint32_t t, int s) {
-        int32_t ci[5], co[5];
-        spg_tma_coords(p, tp, t, ci, co);
-        const uint32_t mb = mbar0 + 8u * (uint32_t)s;
-        spg_mbar_expect_tx(mb, tx);
-        spg_tma_load5(base + (uint32_t)s * sb, &tmap_in, ci, mb);
-        if (spg_reads_out<OP>::value) spg_tma_load5(base + (uint32_t)s * sb + in_bytes, &tmap_out, co, mb);
-        (void)co;
-    };
-
-    if (tid == 0) {
-#pragma unroll
-        for (int q = 0; q < S - 1; ++q) {
-            const uint32_t t = blockIdx.x + (uint32_t)q * G;
-            if (t < p.ntiles) issue(t, q);
-        }
-    }
+    __syncthreads();                        // barriers initialised before anyone waits
     const SpgFactor fac = p.fac;
     bool failed = false;
     int it = 0;

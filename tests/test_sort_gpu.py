@@ -297,3 +297,30 @@ def test_status_form_bad_perm_leaves_output(cuda):
                      (2, 2, 3, 4), 1.0)
     assert rc == 2
     assert torch.all(ds == 3.0)
+
+
+def test_i8_shims(cuda):
+    """-i8 NWChem builds pass 8-byte integers; the _i8 drop-ins narrow them."""
+    import ctypes
+    dims = (7, 30, 9, 16)
+    n = int(np.prod(dims))
+    u = O.fixture_values(n, 90)
+    y = O.fixture_values(n, 91)
+    du = dev(u, cuda)
+    L = lib()
+    r8 = lambda v: ctypes.byref(ctypes.c_int64(v))  # noqa: E731
+    for name, g in (("tce_sort_4_i8", 0.0), ("tce_sortacc_4_i8_", 1.0)):
+        ds = dev(y, cuda)
+        torch.cuda.synchronize()
+        getattr(L, name)(ctypes.c_void_p(du.data_ptr()), ctypes.c_void_p(ds.data_ptr()),
+                         *[r8(d) for d in dims], *[r8(p) for p in (3, 1, 4, 2)],
+                         ctypes.byref(ctypes.c_double(-0.5)))
+        assert L.spaghetty_last_error() == 0
+        check(host(ds), O.np_sort(u, dims, (3, 1, 4, 2), -0.5, g, out=y), name)
+    # out-of-range 8-byte value: rejected, output untouched
+    ds = dev(y, cuda)
+    L.tce_sort_4_i8(ctypes.c_void_p(du.data_ptr()), ctypes.c_void_p(ds.data_ptr()),
+                    r8(1 << 40), r8(30), r8(9), r8(16), r8(3), r8(1), r8(4), r8(2),
+                    ctypes.byref(ctypes.c_double(1.0)))
+    assert L.spaghetty_last_error() == 3
+    check(host(ds), y, "untouched")
