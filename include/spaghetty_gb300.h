@@ -217,6 +217,10 @@ const char *spaghetty_error_string(int code);
  * of staging them through device copies; 0 stages every host buffer.
  * Pageable host buffers are always staged. */
 #define SPAGHETTY_OPT_HOST_ZERO_COPY 1
+/* SPAGHETTY_OPT_HOST_PIPELINE (default 0): when both buffers are pinned
+ * host memory, move them in slabs along the output's slowest index through
+ * a two-stream upload / sort / download pipeline instead. */
+#define SPAGHETTY_OPT_HOST_PIPELINE 2
 int spaghetty_set_option(int option, int value);
 
 /* Synchronise the current device and report (then clear) the kernels'

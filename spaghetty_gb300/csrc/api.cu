@@ -376,6 +376,9 @@ bool overlaps(const double *a, const double *b, int64_t n) {
 // staged with copies.  spaghetty_set_option(SPAGHETTY_OPT_HOST_ZERO_COPY, 0)
 // turns that off (staging for every host buffer).
 int g_zero_copy = 1;
+// Pinned host buffers on both sides may instead be moved in slabs through a
+// two-stream copy/kernel/copy pipeline (SPAGHETTY_OPT_HOST_PIPELINE).
+int g_pipeline = 0;
 
 // Where a pointer lives.  0 = pageable host memory, 1 = memory a kernel on
 // `dev` may access (device or managed), 2 = pinned host memory (its mapped
@@ -434,6 +437,87 @@ struct DeviceGuard {
     }
 };
 
+// Two library streams and two slab buffer pairs per device for the pipeline.
+struct PipeRes {
+    cudaStream_t st[2] = {nullptr, nullptr};
+    double *in[2] = {nullptr, nullptr}, *out[2] = {nullptr, nullptr};
+    size_t cap = 0;
+};
+std::map<int, PipeRes> g_pipe;
+
+// Host buffers moved in slabs along the OUTPUT's slowest index: slab c of
+// the output needs the input elements whose index a = perm[0]-1 lies in the
+// slab's range -- for each of the `outer` combinations of the input indices
+// before a, one contiguous run of (slab width x inner) elements, i.e. one
+// pitched 2-D copy.  The slab is then a smaller sort of the same
+// permutation, and the output slab is contiguous.  Slab c+1's upload runs
+// while slab c is sorted and downloaded (the two copy directions overlap).
+// Returns SPAGHETTY_ERR_CONFIG when the copy rows would be too short to pay.
+int sort_host_pipelined(int rank, const double *u, double *s, const int *dims, const int *perm,
+                        double f, double g, int dev, int sms) {
+    const int a = perm[0] - 1;
+    int64_t n = 1, outer = 1, inner = 1;
+    for (int q = 0; q < rank; ++q) n *= dims[q];
+    for (int q = 0; q < a; ++q) outer *= dims[q];
+    for (int q = a + 1; q < rank; ++q) inner *= dims[q];
+    const int64_t E = dims[a];
+    const int64_t slice = n / E;                       // output elements per index value
+    int64_t cs = std::max<int64_t>(1, ((int64_t)16 << 20) / (slice * 8));   // ~16 MB slabs
+    cs = std::min<int64_t>(cs, std::max<int64_t>(1, (E + 3) / 4));        // at least ~4 slabs
+    if (E < 2 || (outer > 1 && cs * inner * 8 < 4096)) return SPAGHETTY_ERR_CONFIG;
+    const bool acc = g != 0.0;
+    PipeRes &pr = g_pipe[dev];
+    const size_t need = (size_t)(cs * slice);
+    if (!pr.st[0]) {
+        for (int b = 0; b < 2; ++b)
+            if (cudaStreamCreateWithFlags(&pr.st[b], cudaStreamNonBlocking) != cudaSuccess) {
+                cudaGetLastError();
+                return SPAGHETTY_ERR_CUDA;
+            }
+    }
+    if (pr.cap < need) {
+        for (int b = 0; b < 2; ++b) {
+            if (pr.in[b]) cudaFree(pr.in[b]);
+            if (pr.out[b]) cudaFree(pr.out[b]);
+            pr.in[b] = pr.out[b] = nullptr;
+        }
+        pr.cap = 0;
+        for (int b = 0; b < 2; ++b)
+            if (cudaMalloc((void **)&pr.in[b], need * 8) != cudaSuccess ||
+                cudaMalloc((void **)&pr.out[b], need * 8) != cudaSuccess) {
+                cudaGetLastError();
+                return SPAGHETTY_ERR_CUDA;
+            }
+        pr.cap = need;
+    }
+    int sub[SPG_MAXR];
+    for (int q = 0; q < rank; ++q) sub[q] = dims[q];
+    int rc = SPAGHETTY_OK;
+    int c = 0;
+    for (int64_t c0 = 0; c0 < E && rc == SPAGHETTY_OK; c0 += cs, ++c) {
+        const int64_t cn = std::min<int64_t>(cs, E - c0);
+        const int b = c & 1;
+        cudaStream_t st = pr.st[b];
+        const size_t w = (size_t)(cn * inner * 8);
+        if (cudaMemcpy2DAsync(pr.in[b], w, u + c0 * inner, (size_t)(E * inner * 8), w, (size_t)outer,
+                              cudaMemcpyHostToDevice, st) != cudaSuccess) { rc = SPAGHETTY_ERR_CUDA; break; }
+        if (acc && cudaMemcpyAsync(pr.out[b], s + c0 * slice, (size_t)(cn * slice * 8),
+                                   cudaMemcpyHostToDevice, st) != cudaSuccess) { rc = SPAGHETTY_ERR_CUDA; break; }
+        sub[a] = (int)cn;
+        Plan pl;
+        rc = make_plan(rank, sub, perm, f, g, sms, &pl, true);
+        if (rc) break;
+        rc = launch_plan(pl, pr.in[b], pr.out[b], st, dev);
+        if (rc) break;
+        if (cudaMemcpyAsync(s + c0 * slice, pr.out[b], (size_t)(cn * slice * 8), cudaMemcpyDeviceToHost,
+                            st) != cudaSuccess) { rc = SPAGHETTY_ERR_CUDA; break; }
+    }
+    for (int b = 0; b < 2; ++b)
+        if (cudaStreamSynchronize(pr.st[b]) != cudaSuccess) rc = SPAGHETTY_ERR_CUDA;
+    if (rc == SPAGHETTY_ERR_CUDA) cudaGetLastError();
+    return rc ? rc : take_device_status();
+}
+
 int sort_sync(int rank, const double *u, double *s, const int *dims, const int *perm,
               double f, double g) {
     Folded fo;
@@ -461,6 +545,12 @@ int sort_sync(int rank, const double *u, double *s, const int *dims, const int *
     cudaStream_t st = 0;  // legacy default stream: ordered after prior blocking-stream work
     const size_t n = (size_t)fo.nelem;
     const size_t bytes = n * sizeof(double);
+    if (g_pipeline && ku == 2 && ks == 2) {
+        std::lock_guard<std::mutex> lk(g_stage_mu);
+        if (cudaStreamSynchronize(st) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
+        rc = sort_host_pipelined(rank, u, s, dims, perm, f, g, dev, device_sms(dev));
+        if (rc != SPAGHETTY_ERR_CONFIG) return rc;
+    }
     if (ku != 0 && ks != 0) {
         rc = launch_plan(pl, (const double *)mu, (double *)ms, st, dev);
         if (rc) return rc;
@@ -623,6 +713,10 @@ int spaghetty_last_error(void) { return g_last_error; }
 int spaghetty_set_option(int option, int value) {
     if (option == SPAGHETTY_OPT_HOST_ZERO_COPY) {
         g_zero_copy = value ? 1 : 0;
+        return SPAGHETTY_OK;
+    }
+    if (option == SPAGHETTY_OPT_HOST_PIPELINE) {
+        g_pipeline = value ? 1 : 0;
         return SPAGHETTY_OK;
     }
     return SPAGHETTY_ERR_CONFIG;

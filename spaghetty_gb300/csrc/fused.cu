@@ -244,9 +244,8 @@ void fused_box(int R, const int64_t *O, int nl, const int (*order)[SPG_FUSED_MAX
 
 }  // namespace
 
-extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *unsorted,
-                                       const int *dims, const int *perms, const double *factors,
-                                       double *sorted, void *stream) {
+static int fused_pass(int rank, int nsrc, const double *const *unsorted, const int *dims,
+                      const int *perms, const double *factors, double *sorted, void *stream) {
     if (rank < 1 || rank > SPG_FUSED_MAXR) return SPAGHETTY_ERR_RANK;
     if (nsrc < 1 || nsrc > SPG_FUSED_MAXS) return SPAGHETTY_ERR_CONFIG;
     if (!unsorted || !dims || !perms || !factors) return SPAGHETTY_ERR_NULL;
@@ -414,6 +413,44 @@ extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *
                          (cudaStream_t)stream) != cudaSuccess) {
         cudaGetLastError();
         return SPAGHETTY_ERR_CUDA;
+    }
+    return SPAGHETTY_OK;
+}
+
+// The sources are split into passes of consecutive sortaccs (so every
+// element still receives its additions in call order) whose sources share
+// their stride-1 index: one box then gives every source and the output
+// long contiguous runs.  The nine triples sortaccs of one group touch one to
+// three such indices, i.e. one to three passes over t3 instead of nine.
+extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *unsorted,
+                                       const int *dims, const int *perms, const double *factors,
+                                       double *sorted, void *stream) {
+    if (rank < 1 || rank > SPG_FUSED_MAXR) return SPAGHETTY_ERR_RANK;
+    if (nsrc < 1 || nsrc > SPG_FUSED_MAXS) return SPAGHETTY_ERR_CONFIG;
+    if (!unsorted || !dims || !perms || !factors) return SPAGHETTY_ERR_NULL;
+    // output position holding each source's stride-1 index (source dim rank)
+    int fast[SPG_FUSED_MAXS];
+    for (int k = 0; k < nsrc; ++k) {
+        fast[k] = -1;
+        for (int q = 0; q < rank; ++q) {
+            const int p = perms[k * rank + q];
+            if (p < 1 || p > rank) return SPAGHETTY_ERR_PERM;
+            // unit source dims do not count: take the fastest non-unit one
+        }
+        for (int i = rank - 1; i >= 0 && fast[k] < 0; --i) {
+            if (dims[k * rank + i] == 1 && i > 0) continue;
+            for (int q = 0; q < rank; ++q)
+                if (perms[k * rank + q] == i + 1) fast[k] = q;
+        }
+    }
+    int k0 = 0;
+    while (k0 < nsrc) {
+        int k1 = k0 + 1;
+        while (k1 < nsrc && fast[k1] == fast[k0]) ++k1;
+        const int rc = fused_pass(rank, k1 - k0, unsorted + k0, dims + k0 * rank, perms + k0 * rank,
+                                  factors + k0, sorted, stream);
+        if (rc) return rc;
+        k0 = k1;
     }
     return SPAGHETTY_OK;
 }

@@ -69,12 +69,16 @@ def sort_generic(unsorted, sorted, dims: Sequence[int], perm: Sequence[int],
     p = int_array(perm)
     L = lib()
     if _is_cuda_tensor(unsorted) and _is_cuda_tensor(sorted):
+        dev = unsorted.device.index
         if stream is None:
-            stream = torch.cuda.current_stream(unsorted.device).cuda_stream
-        with torch.cuda.device(unsorted.device):
-            rc = L.spaghetty_sort_async(rank, _ptr(unsorted), _ptr(sorted), d, p,
-                                        float(factor), float(acc_factor),
-                                        ctypes.c_void_p(int(stream)))
+            stream = torch.cuda.current_stream(dev).cuda_stream
+        args = (rank, _ptr(unsorted), _ptr(sorted), d, p, float(factor), float(acc_factor),
+                ctypes.c_void_p(int(stream)))
+        if dev == torch.cuda.current_device():
+            rc = L.spaghetty_sort_async(*args)
+        else:
+            with torch.cuda.device(dev):
+                rc = L.spaghetty_sort_async(*args)
     else:
         if _is_cuda_tensor(unsorted) or _is_cuda_tensor(sorted):
             torch.cuda.current_stream().synchronize()

@@ -253,6 +253,17 @@ def test_host_buffers_are_staged(cuda):
         ps = torch.from_numpy(y).pin_memory()
         call_dropin("tce_sortacc_4", pu.data_ptr(), ps.data_ptr(), dims, perm, 0.5)
         check(ps.numpy(), O.np_sort(u, dims, perm, 0.5, 1.0, out=y), ("pinned", perm))
+        # pinned buffers moved in slabs through the copy/sort/copy pipeline
+        assert lib().spaghetty_set_option(2, 1) == 0
+        try:
+            for f, g in ((-0.5, 0.0), (37.0, 1.0)):
+                ps = torch.from_numpy(y).pin_memory()
+                call_dropin("tce_sortacc_4" if g else "tce_sort_4", pu.data_ptr(), ps.data_ptr(),
+                            dims, perm, f)
+                assert lib().spaghetty_last_error() == 0
+                check(ps.numpy(), O.np_sort(u, dims, perm, f, g, out=y), ("pipelined", perm, g))
+        finally:
+            lib().spaghetty_set_option(2, 0)
         # pinned buffers staged through device copies instead of used in place
         assert lib().spaghetty_set_option(1, 0) == 0
         try:
