@@ -298,7 +298,8 @@ def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--sweep", default="sort4", choices=["sort4", "sort6-triples", "case"])
+    ap.add_argument("--sweep", default="sort4",
+                    choices=["sort4", "sort6-triples", "sort6-sample", "case"])
     ap.add_argument("--dims", default="100,100,100,100")
     ap.add_argument("--perm", default="4,3,2,1")
     ap.add_argument("--ops", default="0,1")
@@ -312,6 +313,14 @@ def main():
         probs = [(d, p) for d in SORT4_DIMS for p in PERMS4]
     elif args.sweep == "sort6-triples":
         probs = [((16,) * 6, p) for p in TRIPLES_SORT6]
+    elif args.sweep == "sort6-sample":
+        # the sort6 configuration's bench sample: triples perms at 16^6 and
+        # 20^6, 48 seeded perms at the non-cubic shape
+        import random
+        from .workloads import PERMS6
+        rnd = random.Random(6)
+        probs = ([((16,) * 6, p) for p in TRIPLES_SORT6] + [((20,) * 6, p) for p in TRIPLES_SORT6]
+                 + [((12, 20, 16, 20, 12, 16), p) for p in rnd.sample(PERMS6, 48)])
     else:
         probs = [(tuple(int(x) for x in args.dims.split(",")),
                   tuple(int(x) for x in args.perm.split(",")))]
