@@ -167,7 +167,8 @@ def clear():
 
 def time_case(dims, perm, op, reps=5, device=None, flush_bytes=512 << 20, bufs=None):
     """Median kernel time (s) of one sort on device buffers, L2 flushed
-    before every launch when the tensors are smaller than 2x L2."""
+    before every launch (so that no launch finds the previous one's tail in
+    L2, which would favour some box orders over others)."""
     import torch
     from .sort import sort_generic
     dev = device or torch.device("cuda", torch.cuda.current_device())
@@ -183,8 +184,7 @@ def time_case(dims, perm, op, reps=5, device=None, flush_bytes=512 << 20, bufs=N
     g = 0.0 if op == 0 else (1.0 if op == 1 else 2.0)
     times = []
     for r in range(reps + 1):
-        if n * 16 < 2 * 129 * 1024 * 1024:
-            flush.fill_(1.0)
+        flush.fill_(1.0)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()

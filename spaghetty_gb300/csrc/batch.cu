@@ -27,7 +27,7 @@
 #include <vector>
 
 #define SPG_BATCH_NT 256
-#define SPG_BATCH_EPT 8
+#define SPG_BATCH_EPT 4
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
 #define SPG_BATCH_UNIT_ELEMS 16384
 

@@ -177,7 +177,7 @@ static const int kTRun = 32;      // minimum contiguous doubles per box row
 static const int kVMax = 4096;    // largest box (512 threads x 8)
 static const int kDefaultStages = 3;
 static const int kBatchThreads = 256;
-static const int kBatchEpt = 8;
+static const int kBatchEpt = 4;
 
 static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L, int vmax) {
     for (int d = 0; d < s.R; ++d) L[d] = 1;
