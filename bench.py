@@ -700,8 +700,30 @@ def run_case(args):
                       "plan": S.plan(dims, perm, op)}), flush=True)
 
 
+def run_fused_case(args):
+    """One fused triples group (profiling workload): --fused-case GROUP:EXTENT."""
+    import torch
+    import spaghetty_gb300 as S
+    from spaghetty_gb300.workloads import TRIPLES_SORTACC6
+    g, ext = (int(x) for x in args.fused_case.split(":"))
+    shape = (ext,) * 6
+    dev = torch.device("cuda", 0)
+    t3 = torch.rand(shape, dtype=torch.float64, device=dev) - 0.5
+    srcs = [torch.rand(shape, dtype=torch.float64, device=dev) - 0.5 for _ in range(9)]
+    perms = TRIPLES_SORTACC6[g]
+    facs = [1.0 if k % 3 else -1.0 for k in range(9)]
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(args.warmup):
+        S.sortacc_fused(t3, srcs, perms, facs)
+    t = _timed_events(lambda: S.sortacc_fused(t3, srcs, perms, facs), max(1, args.steps), stream)
+    n = ext ** 6
+    print(json.dumps({"fused_case": args.fused_case, "ms": round(t * 1e3, 4),
+                      "gbs": round((16 * n + 72 * n) / t / 1e9, 1)}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--fused-case", default=None, help="GROUP:EXTENT: time one fused triples group")
     ap.add_argument("--case", default=None,
                     help="dims:perm:op[:factor] (op 0 sort, 1 sortacc; factor 0.5): time one case")
     ap.add_argument("--gpus", type=int, default=1)
@@ -718,6 +740,9 @@ def main():
     ws, rank, local = dist_env()
     if args.case:
         run_case(args)
+        return
+    if args.fused_case:
+        run_fused_case(args)
         return
     if args.impl == "reference":
         line = run_reference(args, ws, rank)
