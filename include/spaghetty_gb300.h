@@ -273,8 +273,8 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
  * with the same folded (dims, perm, op).  box[] is indexed by folded dim;
  * threads in {128,256,512}; ept in {1,2,4,8}; stages in {0,2,3} (tiled
  * kernel: 0 = register-staged, 2/3 = cp.async pipeline depth, needs
- * ept >= 2) or 12/13/14 (TMA-staged kernel with 2/3/4 stages; threads in
- * {128,256}, ept in {8,16}).  Pass box == NULL to clear every override.  Returns a
+ * ept >= 2) or 12/13/14/16 (TMA-staged kernel with 2/3/4/6 load stages;
+ * threads in {128,256}, ept in {8,16}).  Pass box == NULL to clear every override.  Returns a
  * SPAGHETTY_* code. */
 int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op,
                        const int *box, int threads, int ept, int stages);

@@ -143,14 +143,14 @@ def candidates(dims: Sequence[int], perm: Sequence[int], op: int = 0):
             stages = (0,) if (p["kind"] == "direct" or ept < 2) else (0, 2, 3)
             for st in stages:
                 out.append((list(b), nt, ept, st))
-        # TMA-staged kernel (stages 12..14 = 2..4 pipeline stages); the
+        # TMA-staged kernel (stages 12/13/14/16 = 2/3/4/6 load stages); the
         # library rejects boxes that do not fit the bulk tensor copy rules
         if p["kind"] != "direct":
             for nt, ept in itertools.product(TMA_THREADS, TMA_EPTS):
                 cap = nt * ept
                 if cap < vol or cap >= 2 * vol + nt:
                     continue
-                for st in (12, 13, 14):
+                for st in (12, 13, 14, 16):
                     out.append((list(b), nt, ept, st))
     return p, out
 
@@ -285,6 +285,12 @@ def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False):
         return None
     results.sort(key=lambda r: r[0])
     t, (box, nt, ept, st) = results[0]
+    if t_default < t:
+        # the planner's own default beat every candidate: record it
+        d = plan(dims, perm, op)
+        if d["kind"] in ("direct", "tiled", "tma"):
+            t, box, nt, ept = t_default, d["box"], d["threads"], d["ept"]
+            st = d["stages"] + 10 if d["kind"] == "tma" else d["stages"]
     bpe = 16 if op == 0 else 24
     ent = {"box": box, "threads": nt, "ept": ept, "stages": st, "seconds": t,
            "gbs": n * bpe / t / 1e9, "default_seconds": t_default,

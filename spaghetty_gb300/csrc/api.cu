@@ -211,9 +211,9 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
     rc = spg_build_params(pl, f, g);
     if (rc) return rc;
     if (pl->kind == KIND_TILED && allow_tma) {
-        // default TMA plan: its own (smaller) box, 256 threads, 3 stages
-        // when three CTAs fit an SM, else 2; kept only when its unpadded
-        // tile reads at most 2-way bank conflicts in the permute step
+        // default TMA plan: its own (smaller) box, 256 threads; kept only
+        // when its unpadded tile reads at most 2-way bank conflicts in the
+        // permute step
         int box[SPG_MAXR];
         Plan tp;
         if (spg_default_box_tma(fo, sms, box) == SPAGHETTY_OK &&
@@ -221,8 +221,12 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
             spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_TILED &&
             tp.wf_pad0 <= 2 * tp.wf_ideal) {
             TmaLayout tl;
-            if (spg_tma_layout(tp, 3, &tl) == SPAGHETTY_OK) {
-                const int stages = tma_smem_bytes(tl, 3) * 3 <= 228 * 1024 ? 3 : 2;
+            if (spg_tma_layout(tp, 4, &tl) == SPAGHETTY_OK) {
+                // the deepest of 4/3/2 load stages that still lets two CTAs
+                // share an SM
+                int stages = 2;
+                for (int S = 4; S > 2; --S)
+                    if (tma_smem_bytes(tl, S) * 2 <= 228 * 1024) { stages = S; break; }
                 if (to_tma(&tp, 256, 8, stages, false) == SPAGHETTY_OK) *pl = tp;
             }
         }
@@ -299,7 +303,7 @@ int take_device_status() {
 }
 
 int tma_smem_bytes(const TmaLayout &tl, int stages) {
-    return stages * tl.tp.stage_bytes + stages * 8 + 1024;
+    return stages * tl.tp.stage_bytes + 2 * tl.tp.out_bytes + stages * 8 + 1024;
 }
 
 int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) {
@@ -972,12 +976,15 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     int rc = spg_fold(rank, dims, perm, &fo);
     if (rc) return rc;
     if (fo.empty || fo.rank < 2) return SPAGHETTY_ERR_CONFIG;
-    if (threads != 128 && threads != 256 && threads != 512) return SPAGHETTY_ERR_CONFIG;
-    if (ept != 1 && ept != 2 && ept != 4 && ept != 8) return SPAGHETTY_ERR_CONFIG;
-    const bool tma = stages >= 12 && stages <= 14;
-    if (stages != 0 && stages != 2 && stages != 3 && !tma) return SPAGHETTY_ERR_CONFIG;
-    if (stages && ept < 2) return SPAGHETTY_ERR_CONFIG;
-    if (tma && ((threads != 128 && threads != 256) || (ept != 8 && ept != 16))) return SPAGHETTY_ERR_CONFIG;
+    const bool tma = stages == 12 || stages == 13 || stages == 14 || stages == 16;
+    if (tma) {
+        if ((threads != 128 && threads != 256) || (ept != 8 && ept != 16)) return SPAGHETTY_ERR_CONFIG;
+    } else {
+        if (threads != 128 && threads != 256 && threads != 512) return SPAGHETTY_ERR_CONFIG;
+        if (ept != 1 && ept != 2 && ept != 4 && ept != 8) return SPAGHETTY_ERR_CONFIG;
+        if (stages != 0 && stages != 2 && stages != 3) return SPAGHETTY_ERR_CONFIG;
+        if (stages && ept < 2) return SPAGHETTY_ERR_CONFIG;
+    }
     const int opc = op == 0 ? OP_SORT_ANY : (op == 1 ? OP_ACC_ANY : OP_GEN);
     Plan pl;
     rc = spg_plan(fo, opc, box, tma ? 256 : threads, tma ? 16 : ept, tma ? 0 : stages, 152, &pl);

@@ -672,10 +672,11 @@ int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out) {
     const int64_t tile = (int64_t)kp.vol * 8;
     const int64_t tile_al = (tile + 1023) & ~(int64_t)1023;
     const bool reads_out = spg_op_class(pl.op) != 0;
-    // stage = input tile, [old-output tile (sortacc)], output tile
+    // load stage = input tile [+ old-output tile (sortacc)]; two output
+    // slots follow the stages
     out->tp.in_bytes = (int32_t)tile_al;
-    out->tp.out_off = (int32_t)(tile_al * (reads_out ? 2 : 1));
-    out->tp.stage_bytes = (int32_t)(out->tp.out_off + tile_al);
+    out->tp.out_bytes = (int32_t)tile_al;
+    out->tp.stage_bytes = (int32_t)(tile_al * (reads_out ? 2 : 1));
     out->tp.tx_bytes = (int32_t)(tile * (reads_out ? 2 : 1));
     (void)stages;
     return SPAGHETTY_OK;

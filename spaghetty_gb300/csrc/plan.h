@@ -91,9 +91,9 @@ struct TmaParams {
     int8_t out_mdim[SPG_MAXR];
     int32_t in_mul[SPG_MAXR];
     int32_t out_mul[SPG_MAXR];
-    int32_t stage_bytes;          // input tile [+ old-output tile] + output tile
-    int32_t in_bytes;             // one tile, 1024-aligned
-    int32_t out_off;              // offset of the output tile within a stage
+    int32_t stage_bytes;          // one load stage: input tile [+ old-output tile]
+    int32_t in_bytes;             // one tile, 1024-aligned (old-output tile offset)
+    int32_t out_bytes;            // one output slot (two of them follow the stages)
     int32_t tx_bytes;             // bytes the loads of one box deliver
     int *status;                  // error word (bounded waits that timed out)
 };

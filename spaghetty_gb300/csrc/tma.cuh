@@ -11,13 +11,14 @@
 // the factor arithmetic applied; for sortacc the old output box is loaded
 // into the output tile by the same bulk load.
 //
-// Pipeline: S stages, each an input tile, (sortacc) an old-output tile, an
-// output tile and an mbarrier.  Thread 0 issues the loads S-1 boxes ahead
-// and the stores; loads never target a tile a store may still be reading,
-// and a stage's output tile is rewritten only after the store issued S boxes
-// earlier has finished reading it.  Every wait on an mbarrier is bounded: on
-// timeout the kernel records an error in the status word, waits (bounded)
-// for its own transfers in flight, and returns.
+// Pipeline: S load stages, each an input tile, (sortacc) an old-output tile
+// and an mbarrier, and a ring of two output tiles.  Thread 0 keeps every
+// load stage busy (the loads of the next S boxes are in flight while one box
+// is permuted) and issues the stores; a load stage is refilled only after
+// every thread has consumed it, and an output tile is rewritten only after
+// the store issued two boxes earlier has finished reading it.  Every wait on
+// an mbarrier is bounded: on timeout the kernel records an error in the
+// status word, waits (bounded) for its own transfers in flight, and returns.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -108,15 +109,18 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
               const __grid_constant__ CUtensorMap tmap_out,
               const __grid_constant__ KParams p, const __grid_constant__ TmaParams tp) {
     extern __shared__ __align__(1024) unsigned char smem_raw0[];
-    // stage s: input tile at s*stage_bytes, output tile at s*stage_bytes +
-    // in_bytes; the base is rounded up to 1024 bytes (the launch adds 1 KB)
+    // load stage s at s*stage_bytes (input tile, then the old-output tile
+    // for sortacc at +in_bytes); output slot o at S*stage_bytes +
+    // o*out_bytes; then S mbarriers.  The base is rounded up to 1024 bytes
+    // (the launch adds 1 KB).
     const uint32_t raw = (uint32_t)__cvta_generic_to_shared(smem_raw0);
     const uint32_t base = (raw + 1023u) & ~1023u;
     unsigned char *smem_raw = smem_raw0 + (base - raw);
     const uint32_t sb = (uint32_t)tp.stage_bytes;
     const uint32_t in_bytes = (uint32_t)tp.in_bytes;     // old-output tile offset
-    const uint32_t out_off = (uint32_t)tp.out_off;
-    const uint32_t mbar0 = base + (uint32_t)S * sb;
+    const uint32_t ob = (uint32_t)tp.out_bytes;
+    const uint32_t out0 = (uint32_t)S * sb;
+    const uint32_t mbar0 = base + out0 + 2u * ob;
     const uint32_t tid = threadIdx.x;
     const uint32_t G = gridDim.x;
     const uint32_t tx = (uint32_t)tp.tx_bytes;
@@ -131,14 +135,14 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
         (void)co;
     };
 
-    // thread 0 sets up the barriers and puts the first S-1 boxes in flight
-    // before anyone builds tables, so DRAM latency overlaps the prologue
+    // thread 0 sets up the barriers and fills every stage before anyone
+    // builds tables, so DRAM latency overlaps the prologue
     if (tid == 0) {
 #pragma unroll
         for (int s = 0; s < S; ++s) spg_mbar_init(mbar0 + 8u * s, 1u);
         spg_fence_mbar_init();
 #pragma unroll
-        for (int q = 0; q < S - 1; ++q) {
+        for (int q = 0; q < S; ++q) {
             const uint32_t t = blockIdx.x + (uint32_t)q * G;
             if (t < p.ntiles) issue(t, q);
         }
@@ -161,41 +165,41 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     const SpgFactor fac = p.fac;
     bool failed = false;
     int it = 0;
+    // One block barrier per box.  Before it, every thread has consumed load
+    // stage s and written output slot o; thread 0 has also waited until the
+    // store issued one box earlier (the last user of the other slot) has
+    // finished reading.  After it, thread 0 stores box it from slot o and
+    // refills stage s with box it+S.
     for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
         const int s = it % S;
-        if (tid == 0) {
-            // refill the stage box it-1 used: its input (and old-output)
-            // tiles were consumed before the last barrier, and the store of
-            // box it-1 reads only the output tile
-            const uint32_t tn = t + (uint32_t)(S - 1) * G;
-            if (tn < p.ntiles) issue(tn, (it + S - 1) % S);
-        }
+        const int o = it & 1;
         const bool ok = spg_mbar_wait(mbar0 + 8u * (uint32_t)s, (uint32_t)((it / S) & 1));
-        // this stage's output tile was last stored S boxes ago: with at most
-        // S-1 newer stores pending, that one has finished reading it
-        if (tid == 0) spg_bulk_wait_read<S - 1>();
+        if (ok) {
+            const double *tin = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb);
+            const double *told = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb + in_bytes);
+            double *tout = reinterpret_cast<double *>(smem_raw + out0 + (size_t)o * ob);
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                if (smr[k] >= 0) {
+                    const uint32_t e = tid + k * NT;
+                    const double y = spg_reads_out<OP>::value ? told[e] : 0.0;
+                    tout[e] = spg_apply<OP>(tin[smr[k]], y, fac);
+                }
+            }
+            spg_fence_async_smem();         // generic-proxy writes -> visible to the bulk store
+        }
+        if (tid == 0) spg_bulk_wait_read<0>();
         if (__syncthreads_or(!ok)) {         // every thread leaves together
             failed = true;
             break;
         }
-        const double *tin = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb);
-        const double *told = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb + in_bytes);
-        double *tout = reinterpret_cast<double *>(smem_raw + (size_t)s * sb + out_off);
-#pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            if (smr[k] >= 0) {
-                const uint32_t e = tid + k * NT;
-                const double y = spg_reads_out<OP>::value ? told[e] : 0.0;
-                tout[e] = spg_apply<OP>(tin[smr[k]], y, fac);
-            }
-        }
-        spg_fence_async_smem();             // generic-proxy writes -> visible to the bulk store
-        __syncthreads();
         if (tid == 0) {
             int32_t ci[5], co[5];
             spg_tma_coords(p, tp, t, ci, co);
-            spg_tma_store5(&tmap_out, co, base + (uint32_t)s * sb + out_off);
+            spg_tma_store5(&tmap_out, co, base + out0 + (uint32_t)o * ob);
             spg_bulk_commit();
+            const uint32_t tn = t + (uint32_t)S * G;
+            if (tn < p.ntiles) issue(tn, s);
         }
     }
     if (failed) {

@@ -29,7 +29,7 @@ HEADER = """// GENERATED by spaghetty_gb300/generator.py -- do not edit.
 """
 TMA_THREADS = (128, 256)
 TMA_EPTS = (8, 16)
-TMA_STAGES = (2, 3, 4)
+TMA_STAGES = (2, 3, 4, 6)
 
 
 STAGES = (2, 3)
