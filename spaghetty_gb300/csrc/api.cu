@@ -91,13 +91,19 @@ int device_sms(int dev) {
     return sms;
 }
 
+// Threads per CTA of a table entry: the TMA-staged kernel adds a producer
+// warp to its permute threads.
+int block_threads(const SpgKernelEntry *k) {
+    return k->kind == KIND_TMA ? SPG_TMA_BLOCK(k->threads) : k->threads;
+}
+
 int occupancy(const SpgKernelEntry *k, int smem) {
     std::lock_guard<std::mutex> lk(g_mu);
     auto key = std::make_pair(k->fn, smem);
     auto it = g_occ.find(key);
     if (it != g_occ.end()) return it->second;
     int nb = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, k->threads, smem) != cudaSuccess) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k->fn, block_threads(k), smem) != cudaSuccess) {
         cudaGetLastError();
         nb = 1;
     }
@@ -303,7 +309,9 @@ int take_device_status() {
 }
 
 int tma_smem_bytes(const TmaLayout &tl, int stages) {
-    return stages * tl.tp.stage_bytes + 2 * tl.tp.out_bytes + stages * 8 + 1024;
+    // stages, two output slots, the mbarriers (full[stages], done[2],
+    // free[2]) and 1 KB for aligning the base
+    return stages * tl.tp.stage_bytes + 2 * tl.tp.out_bytes + (stages + 4) * 8 + 1024;
 }
 
 int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) {
@@ -342,7 +350,7 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
         if (grid < 1) grid = 1;
         pl.grid = (int)grid;
         void *args[] = {(void *)&mi, (void *)&mo, (void *)&pl.kp, (void *)&tl.tp};
-        err = cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(pl.threads), args, (size_t)smem, st);
+        err = cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(block_threads(k)), args, (size_t)smem, st);
     } else {
         const SpgKernelEntry *k = find_kernel(pl.kind, pl.op, pl.threads, pl.ept, pl.stages);
         if (!k) return SPAGHETTY_ERR_NOKERNEL;

@@ -11,14 +11,16 @@
 // the factor arithmetic applied; for sortacc the old output box is loaded
 // into the output tile by the same bulk load.
 //
-// Pipeline: S load stages, each an input tile, (sortacc) an old-output tile
-// and an mbarrier, and a ring of two output tiles.  Thread 0 keeps every
-// load stage busy (the loads of the next S boxes are in flight while one box
-// is permuted) and issues the stores; a load stage is refilled only after
-// every thread has consumed it, and an output tile is rewritten only after
-// the store issued two boxes earlier has finished reading it.  Every wait on
-// an mbarrier is bounded: on timeout the kernel records an error in the
-// status word, waits (bounded) for its own transfers in flight, and returns.
+// Pipeline (warp-specialised): S load stages, each an input tile,
+// (sortacc) an old-output tile and a "full" mbarrier, and two output slots,
+// each with a "done" mbarrier (the permute threads finished the box) and a
+// "free" mbarrier (the store has read the slot).  One producer thread keeps
+// every load stage busy and issues the stores; the permute threads never
+// meet at a block barrier inside the loop.  A load stage is refilled only
+// after every permute thread has consumed it, and an output slot is
+// rewritten only after the store issued two boxes earlier has read it.
+// Every wait is bounded: on timeout a thread records an error in the status
+// word and leaves; the producer waits (bounded) for its transfers in flight.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -103,16 +105,24 @@ __host__ __device__ __forceinline__ void spg_tma_coords(const KParams &p, const 
     }
 }
 
+__device__ __forceinline__ void spg_mbar_arrive(uint32_t addr) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(addr) : "memory");
+}
+
+// Threads in one CTA of spg_tiled_tma: NT permute threads and one producer
+// warp.
+#define SPG_TMA_BLOCK(NT) ((NT) + 32)
+
 template <int NT, int EPT, int OP, int S>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(SPG_TMA_BLOCK(NT))
 spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
               const __grid_constant__ CUtensorMap tmap_out,
               const __grid_constant__ KParams p, const __grid_constant__ TmaParams tp) {
     extern __shared__ __align__(1024) unsigned char smem_raw0[];
     // load stage s at s*stage_bytes (input tile, then the old-output tile
     // for sortacc at +in_bytes); output slot o at S*stage_bytes +
-    // o*out_bytes; then S mbarriers.  The base is rounded up to 1024 bytes
-    // (the launch adds 1 KB).
+    // o*out_bytes; then the mbarriers: full[S], done[2], free[2].  The base
+    // is rounded up to 1024 bytes (the launch adds 1 KB).
     const uint32_t raw = (uint32_t)__cvta_generic_to_shared(smem_raw0);
     const uint32_t base = (raw + 1023u) & ~1023u;
     unsigned char *smem_raw = smem_raw0 + (base - raw);
@@ -120,41 +130,47 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     const uint32_t in_bytes = (uint32_t)tp.in_bytes;     // old-output tile offset
     const uint32_t ob = (uint32_t)tp.out_bytes;
     const uint32_t out0 = (uint32_t)S * sb;
-    const uint32_t mbar0 = base + out0 + 2u * ob;
+    const uint32_t full0 = base + out0 + 2u * ob;        // loads of a stage landed
+    const uint32_t done0 = full0 + 8u * S;               // permute threads finished a box
+    const uint32_t free0 = done0 + 16u;                  // store finished reading a slot
     const uint32_t tid = threadIdx.x;
     const uint32_t G = gridDim.x;
-    const uint32_t tx = (uint32_t)tp.tx_bytes;
 
     auto issue = [&](uint32_t t, int s) {
         int32_t ci[5], co[5];
         spg_tma_coords(p, tp, t, ci, co);
-        const uint32_t mb = mbar0 + 8u * (uint32_t)s;
-        spg_mbar_expect_tx(mb, tx);
+        const uint32_t mb = full0 + 8u * (uint32_t)s;
+        spg_mbar_expect_tx(mb, (uint32_t)tp.tx_bytes);
         spg_tma_load5(base + (uint32_t)s * sb, &tmap_in, ci, mb);
         if (spg_reads_out<OP>::value) spg_tma_load5(base + (uint32_t)s * sb + in_bytes, &tmap_out, co, mb);
         (void)co;
     };
-
-    // thread 0 sets up the barriers and fills every stage before anyone
-    // builds tables, so DRAM latency overlaps the prologue
-    if (tid == 0) {
+    // the producer thread sets up the barriers and fills every stage before
+    // the permute threads build their tables, so DRAM latency overlaps the
+    // prologue
+    int issued = 0;                         // producer: boxes whose loads were issued
+    if (tid == NT) {
 #pragma unroll
-        for (int s = 0; s < S; ++s) spg_mbar_init(mbar0 + 8u * s, 1u);
+        for (int s = 0; s < S; ++s) spg_mbar_init(full0 + 8u * s, 1u);
+#pragma unroll
+        for (int o = 0; o < 2; ++o) {
+            spg_mbar_init(done0 + 8u * o, (uint32_t)(NT / 32));
+            spg_mbar_init(free0 + 8u * o, 1u);
+        }
         spg_fence_mbar_init();
-#pragma unroll
         for (int q = 0; q < S; ++q) {
             const uint32_t t = blockIdx.x + (uint32_t)q * G;
-            if (t < p.ntiles) issue(t, q);
+            if (t < p.ntiles) { issue(t, q); ++issued; }
         }
     }
-    // element tables: output-tile element e = tid + k*NT takes input-tile
-    // element smr[k]
+    // permute-thread tables: output-tile element e = tid + k*NT takes
+    // input-tile element smr[k]
     int32_t smr[EPT];
 #pragma unroll
     for (int k = 0; k < EPT; ++k) {
         const uint32_t e = tid + k * NT;
         smr[k] = -1;
-        if (e < (uint32_t)p.vol) {
+        if (tid < NT && e < (uint32_t)p.vol) {
             int32_t a, b, lin;
             uint32_t pk;
             spg_walk(p.st, e, a, b, lin, pk);
@@ -162,58 +178,70 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
         }
     }
     __syncthreads();                        // barriers initialised before anyone waits
-    const SpgFactor fac = p.fac;
-    bool failed = false;
-    int it = 0;
-    // One block barrier per box.  Before it, every thread has consumed load
-    // stage s and written output slot o; thread 0 has also waited until the
-    // store issued one box earlier (the last user of the other slot) has
-    // finished reading.  After it, thread 0 stores box it from slot o and
-    // refills stage s with box it+S.
-    for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
-        const int s = it % S;
-        const int o = it & 1;
-        const bool ok = spg_mbar_wait(mbar0 + 8u * (uint32_t)s, (uint32_t)((it / S) & 1));
-        if (ok) {
-            const double *tin = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb);
-            const double *told = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb + in_bytes);
-            double *tout = reinterpret_cast<double *>(smem_raw + out0 + (size_t)o * ob);
-#pragma unroll
-            for (int k = 0; k < EPT; ++k) {
-                if (smr[k] >= 0) {
-                    const uint32_t e = tid + k * NT;
-                    const double y = spg_reads_out<OP>::value ? told[e] : 0.0;
-                    tout[e] = spg_apply<OP>(tin[smr[k]], y, fac);
-                }
-            }
-            spg_fence_async_smem();         // generic-proxy writes -> visible to the bulk store
-        }
-        if (tid == 0) spg_bulk_wait_read<0>();
-        if (__syncthreads_or(!ok)) {         // every thread leaves together
-            failed = true;
-            break;
-        }
-        if (tid == 0) {
+
+    if (tid >= NT) {
+        // ---- producer: one thread issues every bulk copy ----
+        if (tid != NT) return;
+        int it = 0;
+        bool ok = true;
+        for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
+            const int s = it % S;
+            const int o = it & 1;
+            // the permute threads have read stage s and written slot o
+            ok = spg_mbar_wait(done0 + 8u * (uint32_t)o, (uint32_t)((it >> 1) & 1));
+            if (!ok) break;
             int32_t ci[5], co[5];
             spg_tma_coords(p, tp, t, ci, co);
             spg_tma_store5(&tmap_out, co, base + out0 + (uint32_t)o * ob);
             spg_bulk_commit();
             const uint32_t tn = t + (uint32_t)S * G;
-            if (tn < p.ntiles) issue(tn, s);
+            if (tn < p.ntiles) { issue(tn, s); ++issued; }
+            // slot o is free again once this store has read it
+            spg_bulk_wait_read<0>();
+            spg_mbar_arrive(free0 + 8u * (uint32_t)o);
         }
-    }
-    if (failed) {
-        if (tid == 0) spg_bulk_wait0();     // stores already issued finish reading
-        if (tid == 0 && tp.status) {
-            *(volatile int *)tp.status = 1;
-            // bounded wait for this CTA's own loads still in flight
-            for (int q = 0; q < S; ++q) {
-                const uint32_t mb = mbar0 + 8u * (uint32_t)q;
-                for (uint32_t i = 0; i < 1024u && !spg_mbar_try_wait(mb, 0u) && !spg_mbar_try_wait(mb, 1u); ++i) {
+        spg_bulk_wait0();                   // stores complete before the CTA retires
+        if (!ok) {
+            if (tp.status) *(volatile int *)tp.status = 1;
+            // bounded wait for the loads still in flight (boxes it..issued-1)
+            for (int j = it; j < issued; ++j) {
+                const uint32_t mb = full0 + 8u * (uint32_t)(j % S);
+                for (uint32_t i = 0; i < 4096u && !spg_mbar_try_wait(mb, (uint32_t)((j / S) & 1)); ++i) {
                 }
             }
         }
         return;
     }
-    if (tid == 0) spg_bulk_wait0();         // stores complete before the CTA retires
+
+    // ---- permute threads ----
+    const SpgFactor fac = p.fac;
+    const uint32_t lane = tid & 31u;
+    int it = 0;
+    for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
+        const int s = it % S;
+        const int o = it & 1;
+        // box it's loads have landed, and the store two boxes back has
+        // finished reading slot o (a fresh barrier passes parity 1)
+        bool ok = spg_mbar_wait(full0 + 8u * (uint32_t)s, (uint32_t)((it / S) & 1)) &&
+                  spg_mbar_wait(free0 + 8u * (uint32_t)o, (uint32_t)(((it >> 1) & 1) ^ 1));
+        ok = __all_sync(0xffffffffu, ok);   // a warp leaves as a whole
+        if (!ok) {
+            if (tp.status) *(volatile int *)tp.status = 1;
+            break;
+        }
+        const double *tin = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb);
+        const double *told = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb + in_bytes);
+        double *tout = reinterpret_cast<double *>(smem_raw + out0 + (size_t)o * ob);
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            if (smr[k] >= 0) {
+                const uint32_t e = tid + k * NT;
+                const double y = spg_reads_out<OP>::value ? told[e] : 0.0;
+                tout[e] = spg_apply<OP>(tin[smr[k]], y, fac);
+            }
+        }
+        spg_fence_async_smem();             // generic-proxy writes -> visible to the bulk store
+        __syncwarp();
+        if (lane == 0) spg_mbar_arrive(done0 + 8u * (uint32_t)o);
+    }
 }
