@@ -145,13 +145,12 @@ def candidates(dims: Sequence[int], perm: Sequence[int], op: int = 0):
                 out.append((list(b), nt, ept, st))
         # TMA-staged kernel (stages 12/13/14/16 = 2/3/4/6 load stages); the
         # library rejects boxes that do not fit the bulk tensor copy rules
-        if p["kind"] != "direct":
-            for nt, ept in itertools.product(TMA_THREADS, TMA_EPTS):
-                cap = nt * ept
-                if cap < vol or cap >= 2 * vol + nt:
-                    continue
-                for st in (12, 13, 14, 16):
-                    out.append((list(b), nt, ept, st))
+        for nt, ept in itertools.product(TMA_THREADS, TMA_EPTS):
+            cap = nt * ept
+            if cap < vol or cap >= 2 * vol + nt:
+                continue
+            for st in (12, 13, 14, 16):
+                out.append((list(b), nt, ept, st))
     return p, out
 
 

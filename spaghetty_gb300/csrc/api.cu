@@ -173,7 +173,7 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
 // Switch a built tiled plan to the TMA-staged kernel with the given shape.
 int to_tma(Plan *pl, int threads, int ept, int stages, bool strict) {
     TmaLayout tl;
-    if (pl->kind != KIND_TILED || threads * ept < pl->kp.vol ||
+    if ((pl->kind != KIND_TILED && pl->kind != KIND_DIRECT) || threads * ept < pl->kp.vol ||
         spg_tma_layout(*pl, stages, &tl) != SPAGHETTY_OK ||
         tma_smem_bytes(tl, stages) > kMaxSmemPerBlock)
         return strict ? SPAGHETTY_ERR_CONFIG : SPAGHETTY_ERR_NOKERNEL;
@@ -839,6 +839,7 @@ static int verify_tma(const Plan &pl, int64_t *stats) {
             int32_t a, b, lin;
             uint32_t pk;
             spg_walk(kp.st, e, a, b, lin, pk);
+            if (tl.tp.same_order) lin = (int32_t)e;
             if (lin < 0 || lin >= kp.vol) return SPAGHETTY_ERR_CONFIG;
             int64_t remi = lin, ig = 0;
             bool iin = true;
@@ -1001,7 +1002,8 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     if (rc) return rc;
     if (tma) {
         TmaLayout tl;
-        if (pl.kind != KIND_TILED || threads * ept < pl.kp.vol || spg_tma_layout(pl, stages - 10, &tl) ||
+        if ((pl.kind != KIND_TILED && pl.kind != KIND_DIRECT) || threads * ept < pl.kp.vol ||
+            spg_tma_layout(pl, stages - 10, &tl) ||
             tma_smem_bytes(tl, stages - 10) > kMaxSmemPerBlock)
             return SPAGHETTY_ERR_CONFIG;
     }

@@ -584,7 +584,9 @@ static int tma_map(const Plan &pl, const int *order, const int64_t *gstride, int
         const int64_t D = fo.D[d];
         const int64_t L = pl.box[d];
         bool merge = false;
-        if (m >= 0) {
+        // a dim joins the group only where it continues the group's memory
+        // range (its stride is the group's stride times the group's extent)
+        if (m >= 0 && (uint64_t)gstride[d] * 8u == stride[m] * dim[m]) {
             if (group_full) merge = true;
             else if (group_unit && L == 1) merge = true;
         }
@@ -638,8 +640,16 @@ int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out) {
         for (int q = R - 1; q >= 0; --q) { op[q] = so; so *= fo.D[fo.P[q]]; }
         for (int d = 0; d < R; ++d) ostr[d] = op[pinv[d]];
     }
+    // When the stride-1 index is the same on both sides, the output map
+    // lists its dims in INPUT order (each with its output stride): the tile
+    // is then laid out identically for the load and the store, and the
+    // permute step is the identity.
+    const bool same_order = fo.P[R - 1] == R - 1;
     int in_order[SPG_MAXR], out_order[SPG_MAXR];
-    for (int q = 0; q < R; ++q) { in_order[q] = R - 1 - q; out_order[q] = fo.P[R - 1 - q]; }
+    for (int q = 0; q < R; ++q) {
+        in_order[q] = R - 1 - q;
+        out_order[q] = same_order ? R - 1 - q : fo.P[R - 1 - q];
+    }
     int8_t mi[SPG_MAXR], mo[SPG_MAXR];
     int64_t wi[SPG_MAXR], wo[SPG_MAXR];
     int rc = tma_map(pl, in_order, istr, &out->rank_in, out->in_dim, out->in_stride, out->in_box, mi, wi);
@@ -678,6 +688,7 @@ int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out) {
     out->tp.out_bytes = (int32_t)tile_al;
     out->tp.stage_bytes = (int32_t)(tile_al * (reads_out ? 2 : 1));
     out->tp.tx_bytes = (int32_t)(tile * (reads_out ? 2 : 1));
+    out->tp.same_order = same_order ? 1 : 0;
     (void)stages;
     return SPAGHETTY_OK;
 }

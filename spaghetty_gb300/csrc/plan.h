@@ -95,6 +95,7 @@ struct TmaParams {
     int32_t in_bytes;             // one tile, 1024-aligned (old-output tile offset)
     int32_t out_bytes;            // one output slot (two of them follow the stages)
     int32_t tx_bytes;             // bytes the loads of one box deliver
+    int32_t same_order;           // 1: both maps list the dims in input order (identity permute)
     int *status;                  // error word (bounded waits that timed out)
 };
 

@@ -174,7 +174,7 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
             int32_t a, b, lin;
             uint32_t pk;
             spg_walk(p.st, e, a, b, lin, pk);
-            smr[k] = lin;
+            smr[k] = tp.same_order ? (int32_t)e : lin;
         }
     }
     __syncthreads();                        // barriers initialised before anyone waits

@@ -177,3 +177,36 @@ def test_tune_set_validation():
     assert verify((30, 30, 30, 30), (4, 3, 2, 1))[0] == 0
     assert L.spaghetty_tune_set(0, None, None, 0, None, 0, 0, 0) == 0   # clear
     assert plan((30, 30, 30, 30), (4, 3, 2, 1))["box"] != [15, 1, 1, 15]
+
+
+def test_tma_candidates_replay_rank4():
+    """Every TMA-staged candidate the tuner can force is replayed on the host.
+    Perms that keep the stride-1 index get the same-order layout (identity
+    permute step, output map listed in input order)."""
+    from spaghetty_gb300.autotune import candidates, clear
+    L = lib()
+    same_order_seen = 0
+    try:
+        for dims in [(10, 12, 14, 16), (6, 20, 9, 34)]:
+            for perm in itertools.permutations((1, 2, 3, 4)):
+                for op in (0, 1):
+                    _, cands = candidates(dims, perm, op)
+                    for box, nt, ept, st in cands:
+                        if st < 12:
+                            continue
+                        rc = L.spaghetty_tune_set(4, int_array(dims), int_array(perm), op,
+                                                  int_array(box), nt, ept, st)
+                        assert rc in (0, 9, 12), (dims, perm, box, rc)
+                        if rc:
+                            continue
+                        p = plan(dims, perm, op)
+                        assert p["kind"] == "tma" and p["stages"] == st - 10
+                        assert p["smem_bytes"] <= 232448
+                        vrc, _ = verify(dims, perm, op)
+                        assert vrc == 0, (dims, perm, op, box, nt, ept, st)
+                        if perm[-1] == 4:
+                            same_order_seen += 1
+                    clear()
+    finally:
+        clear()
+    assert same_order_seen > 0

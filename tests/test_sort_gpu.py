@@ -335,3 +335,40 @@ def test_i8_shims(cuda):
                     ctypes.byref(ctypes.c_double(1.0)))
     assert L.spaghetty_last_error() == 3
     check(host(ds), y, "untouched")
+
+
+@pytest.mark.parametrize("dims", [(6, 20, 9, 34), (10, 12, 14, 16)])
+def test_every_forced_variant_rank4(cuda, dims):
+    """Every (box, block shape, pipeline) the tuner can force, TMA-staged
+    kernels with 2/3/4/6 load stages and the same-order layout included,
+    gives the oracle's bits for every perm, sort and sortacc."""
+    from spaghetty_gb300.autotune import candidates, clear
+    L = lib()
+    n = int(np.prod(dims))
+    u = O.seeded_uniform(n, 21)
+    y = O.seeded_uniform(n, 22)
+    du, dy = dev(u, cuda), dev(y, cuda)
+    ran = {"tma": 0, "other": 0}
+    try:
+        for perm in itertools.permutations((1, 2, 3, 4)):
+            for op, f in ((0, -0.5), (1, 0.75)):
+                g = float(op)
+                want = dev(O.np_sort(u, dims, perm, f, g, out=y), cuda)
+                _, cands = candidates(dims, perm, op)
+                for box, nt, ept, st in cands:
+                    if L.spaghetty_tune_set(4, int_array(dims), int_array(perm), op,
+                                            int_array(box), nt, ept, st) != 0:
+                        continue
+                    s = dy.clone()
+                    sort_generic(du, s, dims, perm, f, g)
+                    torch.cuda.synchronize()
+                    if not torch.equal(s, want):
+                        pytest.fail("variant %s: mismatch %s" % (
+                            (dims, perm, op, box, nt, ept, st),
+                            first_mismatch(s.cpu().numpy(), want.cpu().numpy())))
+                    ran["tma" if st >= 12 else "other"] += 1
+                clear()
+    finally:
+        clear()
+    assert ran["tma"] > 0 and ran["other"] > 0
+    assert lib().spaghetty_device_status() == 0
