@@ -569,9 +569,12 @@ int spg_selftest_host(void) {
 // tensor-map dims: a slower dim joins the current group when every dim
 // already in it is covered by the box in full (the group is then one
 // contiguous range), or when it and every dim already in the group have
-// box length 1.  Box lengths along a map dim are at most 256, the innermost
-// box row is a multiple of 16 bytes, and every stride a multiple of 16 bytes
-// (the bulk tensor copy's rules); otherwise the plan is not TMA-eligible.
+// box length 1, and in both cases only when its stride continues the
+// group's memory range.  A dim whose box is longer than 256 elements is
+// split into two map dims.  Box lengths along a map dim are at most 256, the
+// innermost box row is a multiple of 16 bytes, and every stride a multiple
+// of 16 bytes (the bulk tensor copy's rules); otherwise the plan is not
+// TMA-eligible.
 static int tma_map(const Plan &pl, const int *order, const int64_t *gstride, int *nmap,
                    uint64_t *dim, uint64_t *stride, uint32_t *box, int8_t *mdim_of,
                    int64_t *weight_of) {
@@ -596,6 +599,27 @@ static int tma_map(const Plan &pl, const int *order, const int64_t *gstride, int
             box[m] = (uint32_t)((int64_t)box[m] * L);
             group_full = group_full && (L == D);
             group_unit = group_unit && (L == 1);
+        } else if (L > 256) {
+            // a box row longer than the bulk copy allows: split the dim into
+            // an inner map dim of w elements (whole box rows of w) and an
+            // outer one, w dividing both the box length and the extent; the
+            // outer coordinate is the element offset / w (weight -w)
+            int64_t w = 256;
+            const bool inner = (m < 0);
+            for (; w > 1; --w)
+                if (L % w == 0 && D % w == 0 && (!inner || (w * 8) % 16 == 0)) break;
+            if (w <= 1 || m + 2 >= 5) return SPAGHETTY_ERR_NOKERNEL;
+            ++m;
+            dim[m] = (uint64_t)w;
+            box[m] = (uint32_t)w;
+            stride[m] = (uint64_t)gstride[d] * 8u;
+            ++m;
+            dim[m] = (uint64_t)(D / w);
+            box[m] = (uint32_t)(L / w);
+            stride[m] = (uint64_t)gstride[d] * 8u * (uint64_t)w;
+            weight_of[d] = -w;
+            group_full = (L == D);
+            group_unit = false;
         } else {
             if (++m >= 5) return SPAGHETTY_ERR_NOKERNEL;
             dim[m] = (uint64_t)D;
@@ -665,7 +689,10 @@ int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out) {
         const int d = gdims[gi];
         const int64_t c = (fo.D[d] + pl.box[d] - 1) / pl.box[d];
         if (k >= kp.grid.n) return SPAGHETTY_ERR_CONFIG;
-        const int64_t mul_in = (int64_t)pl.box[d] * wi[d], mul_out = (int64_t)pl.box[d] * wo[d];
+        // coordinate step of one box along d (a split dim moves its outer
+        // map dim by box / w)
+        const int64_t mul_in = wi[d] > 0 ? (int64_t)pl.box[d] * wi[d] : (int64_t)pl.box[d] / -wi[d];
+        const int64_t mul_out = wo[d] > 0 ? (int64_t)pl.box[d] * wo[d] : (int64_t)pl.box[d] / -wo[d];
         if (mul_in * c > INT32_MAX || mul_out * c > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
         out->tp.in_mdim[k] = mi[d];
         out->tp.out_mdim[k] = mo[d];

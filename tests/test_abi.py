@@ -187,7 +187,7 @@ def test_tma_candidates_replay_rank4():
     L = lib()
     same_order_seen = 0
     try:
-        for dims in [(10, 12, 14, 16), (6, 20, 9, 34)]:
+        for dims in [(10, 12, 14, 16), (6, 20, 9, 34), (4, 6, 50, 40)]:
             for perm in itertools.permutations((1, 2, 3, 4)):
                 for op in (0, 1):
                     _, cands = candidates(dims, perm, op)
