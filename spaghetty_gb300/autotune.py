@@ -294,8 +294,8 @@ def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False):
     best_tma = min((r[0] for r in results if r[1][3] >= 12), default=None)
     best_other = min((r[0] for r in results if r[1][3] < 12), default=None)
     ent = {"box": box, "threads": nt, "ept": ept, "stages": st, "seconds": t,
-           "best_tma_gbs": n * (16 if op == 0 else 24) / best_tma / 1e9 if best_tma else None,
-           "best_other_gbs": n * (16 if op == 0 else 24) / best_other / 1e9 if best_other else None,
+           "best_tma_gbs": n * bpe / best_tma / 1e9 if best_tma else None,
+           "best_other_gbs": n * bpe / best_other / 1e9 if best_other else None,
            "gbs": n * bpe / t / 1e9, "default_seconds": t_default,
            "default_gbs": n * bpe / t_default / 1e9, "candidates": len(results),
            "good": sum(1 for r in results if r[0] < 1.2 * t)}
