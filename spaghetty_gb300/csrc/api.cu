@@ -91,8 +91,8 @@ int device_sms(int dev) {
     return sms;
 }
 
-// Threads per CTA of a table entry: the TMA-staged kernel adds a producer
-// warp to its permute threads.
+// Threads per CTA of a table entry: the TMA-staged kernel adds a load warp
+// and a store warp to its permute threads.
 int block_threads(const SpgKernelEntry *k) {
     return k->kind == KIND_TMA ? SPG_TMA_BLOCK(k->threads) : k->threads;
 }
@@ -309,9 +309,9 @@ int take_device_status() {
 }
 
 int tma_smem_bytes(const TmaLayout &tl, int stages) {
-    // stages, two output slots, the mbarriers (full[stages], done[2],
-    // free[2]) and 1 KB for aligning the base
-    return stages * tl.tp.stage_bytes + 2 * tl.tp.out_bytes + (stages + 4) * 8 + 1024;
+    // stages, two output slots, the mbarriers (full[stages], empty[stages],
+    // done[2], free[2]) and 1 KB for aligning the base
+    return stages * tl.tp.stage_bytes + 2 * tl.tp.out_bytes + (2 * stages + 4) * 8 + 1024;
 }
 
 int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) {

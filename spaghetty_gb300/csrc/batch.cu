@@ -30,6 +30,12 @@
 #define SPG_BATCH_EPT 4
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
 #define SPG_BATCH_UNIT_ELEMS 16384
+#ifndef SPG_BATCH_S
+#define SPG_BATCH_S 3          // cp.async stages of the tiled path
+#endif
+#ifndef SPG_BATCH_DIRECT2
+#define SPG_BATCH_DIRECT2 1    // direct sorts: two boxes in flight per step
+#endif
 
 struct BatchJob {
     KParams kp;
@@ -41,20 +47,117 @@ struct BatchJob {
     uint32_t chunk;    // boxes per work unit
 };
 
+// Dynamic shared memory of one launch: SPG_BATCH_S stages of the largest
+// stage size (elements) among the batch's tiled sorts.
+static inline size_t batch_smem_bytes(int stage_elems) {
+    return (size_t)SPG_BATCH_S * (size_t)stage_elems * sizeof(double);
+}
+
 // Status word bits.
 #define SPG_ST_BAD_JOB 1
 #define SPG_ST_BAD_UNIT 2
 
+// Boxes [b0, b1) of one tiled sort, pipelined: 8-byte cp.async copies put
+// box t+S-1 in flight (SPG_BATCH_S stages of the sort's stage size) while
+// box t is written out in output order.  Every thread of the CTA calls it
+// with the same arguments; nothing is left in flight when it returns.
+template <int OP>
+__device__ __forceinline__ void spg_batch_tiled(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
+                                                uint32_t b0, uint32_t b1, double *sm) {
+    const KParams &p = j.kp;
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
+    const uint32_t stage_bytes = (uint32_t)p.stage * 8u;
+    const double *in = j.in;
+    auto issue = [&](uint32_t t, int st) {
+        if (t < b1) {
+            int64_t ib, ob;
+            uint32_t limA, limB;
+            spg_box(p, t, ib, ob, limA, limB);
+            const double *src = in + ib;
+            const uint32_t sb = sbase + (uint32_t)st * stage_bytes;
+#pragma unroll
+            for (int k = 0; k < SPG_BATCH_EPT; ++k) {
+                if (tb.pkl[k] != SPG_INVALID) {
+                    const bool v = spg_valid(tb.pkl[k], limA, limB);
+                    spg_cp_async8(sb + (uint32_t)tb.smw[k] * 8u, v ? src + tb.ioff[k] : in, v ? 8u : 0u);
+                }
+            }
+        }
+        spg_cp_commit();
+    };
+    const SpgFactor fac = p.fac;
+#pragma unroll
+    for (int q = 0; q < SPG_BATCH_S - 1; ++q) issue(b0 + (uint32_t)q, q);
+    int it = 0;
+    for (uint32_t t = b0; t < b1; ++t, ++it) {
+        const int st = it % SPG_BATCH_S;
+        __syncthreads();                       // the stage refilled below is no longer read
+        issue(t + SPG_BATCH_S - 1, (it + SPG_BATCH_S - 1) % SPG_BATCH_S);
+        spg_cp_wait<SPG_BATCH_S - 1>();        // this thread's copies for box t have landed
+        __syncthreads();                       // ... and everyone else's
+        int64_t ib, ob;
+        uint32_t limA, limB;
+        spg_box(p, t, ib, ob, limA, limB);
+        double *dst = j.out + ob;
+        const double *tile = sm + (size_t)st * p.stage;
+        double y[SPG_BATCH_EPT];
+        if (spg_reads_out<OP>::value) {
+#pragma unroll
+            for (int k = 0; k < SPG_BATCH_EPT; ++k) {
+                y[k] = 0.0;
+                if (spg_valid(tb.pks[k], limA, limB)) y[k] = spg_ld_out(dst + tb.ooff[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < SPG_BATCH_EPT; ++k) {
+            if (spg_valid(tb.pks[k], limA, limB)) {
+                const double x = tile[tb.smr[k]];
+                spg_st_out(dst + tb.ooff[k], spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, fac));
+            }
+        }
+    }
+    spg_cp_wait<0>();
+}
+
+// Boxes [b0, b1) of one direct sort, two boxes per step so that twice the
+// loads are in flight.
+template <int OP>
+__device__ __forceinline__ void spg_batch_direct(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
+                                                 uint32_t b0, uint32_t b1) {
+    const KParams &p = j.kp;
+    const SpgFactor fac = p.fac;
+    uint32_t t = b0;
+    for (; SPG_BATCH_DIRECT2 && t + 1 < b1; t += 2) {
+        int64_t ib[2], ob[2];
+        uint32_t lA[2], lB[2];
+        spg_box(p, t, ib[0], ob[0], lA[0], lB[0]);
+        spg_box(p, t + 1, ib[1], ob[1], lA[1], lB[1]);
+        double v[2][SPG_BATCH_EPT], y[2][SPG_BATCH_EPT];
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int k = 0; k < SPG_BATCH_EPT; ++k) {
+                v[h][k] = 0.0; y[h][k] = 0.0;
+                if (spg_valid(tb.pkl[k], lA[h], lB[h])) {
+                    v[h][k] = spg_ld_in(j.in + ib[h] + tb.ioff[k]);
+                    if (spg_reads_out<OP>::value) y[h][k] = spg_ld_out(j.out + ob[h] + tb.ooff[k]);
+                }
+            }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+#pragma unroll
+            for (int k = 0; k < SPG_BATCH_EPT; ++k)
+                if (spg_valid(tb.pkl[k], lA[h], lB[h]))
+                    spg_st_out(j.out + ob[h] + tb.ooff[k], spg_apply<OP>(v[h][k], y[h][k], fac));
+    }
+    if (t < b1) spg_direct_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(p, tb, j.in, j.out, t);
+}
+
 template <int OP>
 __device__ __forceinline__ void spg_batch_units(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
                                                 uint32_t b0, uint32_t b1, double *sm) {
-    if (j.kind == KIND_TILED) {
-        for (uint32_t t = b0; t < b1; ++t)
-            spg_tiled_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(j.kp, tb, j.in, j.out, t, sm);
-    } else {
-        for (uint32_t t = b0; t < b1; ++t)
-            spg_direct_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(j.kp, tb, j.in, j.out, t);
-    }
+    if (j.kind == KIND_TILED) spg_batch_tiled<OP>(j, tb, b0, b1, sm);
+    else spg_batch_direct<OP>(j, tb, b0, b1);
 }
 
 __global__ void __launch_bounds__(SPG_BATCH_NT)
@@ -89,12 +192,15 @@ spg_batched(const BatchJob *__restrict__ jobs, uint32_t njobs,
             if (tid == 0) {
                 const KParams &p = sj.kp;
                 const int tile = p.vol + (p.pad > 0 ? p.vol / p.pad + 1 : 0);
+                // the stages: SPG_BATCH_S of the sort's stage size fit the
+                // dynamic shared memory (smem_elems per stage)
                 bool ok = (sj.kind == KIND_TILED || sj.kind == KIND_DIRECT) && sj.op >= 0 &&
                           sj.op < OP_COUNT && p.vol >= 1 && p.vol <= SPG_BATCH_VMAX &&
                           p.pad >= 0 && sj.in != nullptr && sj.out != nullptr && sj.chunk >= 1 &&
                           p.ntiles >= 1 && p.ld.n >= 0 && p.ld.n <= SPG_MAXR && p.st.n >= 0 &&
                           p.st.n <= SPG_MAXR && p.grid.n >= 0 && p.grid.n <= SPG_MAXR &&
-                          (sj.kind != KIND_TILED || tile <= smem_elems) && u >= sj.ubeg;
+                          (sj.kind != KIND_TILED || (tile <= p.stage && p.stage <= smem_elems)) &&
+                          u >= sj.ubeg;
                 s_ok = ok ? 1 : 0;
                 if (!ok) atomicOr(status, SPG_ST_BAD_JOB);
             }
@@ -130,7 +236,7 @@ struct spaghetty_batch {
     int n = 0;
     uint32_t njobs = 0;
     uint32_t total_units = 0;
-    int smem_elems = 0;
+    int smem_elems = 0;               // stage size (elements) of the largest tiled sort
     BatchJob *d_jobs = nullptr;
     uint32_t *d_unit_job = nullptr;
     uint32_t *d_words = nullptr;      // [0] = unit counter, [1] = status word
@@ -159,7 +265,7 @@ bool is_device_ptr(const void *p, int *dev) {
 int grid_for(spaghetty_batch *b) {
     int sms = 0, nb = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->dev) != cudaSuccess) sms = 152;
-    const size_t smem = (size_t)b->smem_elems * sizeof(double);
+    const size_t smem = batch_smem_bytes(b->smem_elems);
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, spg_batched, SPG_BATCH_NT, smem) != cudaSuccess ||
         nb < 1)
         nb = 1;
@@ -224,7 +330,7 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         if ((uint64_t)unit_job.size() + units > 0xFFFFFFF0ull) { rc = SPAGHETTY_ERR_OVERFLOW; break; }
         for (uint32_t q = 0; q < units; ++q) unit_job.push_back((uint32_t)b->jobs.size());
         if (pl.kind == KIND_TILED)
-            b->smem_elems = std::max(b->smem_elems, pl.kp.vol + (pl.kp.pad ? pl.kp.vol / pl.kp.pad + 1 : 0));
+            b->smem_elems = std::max(b->smem_elems, (int)pl.kp.stage);
         b->bytes += fo.nelem * (spg_op_class(op) == 0 ? 16 : 24);
         b->jobs.push_back(j);
     }
@@ -266,9 +372,9 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         spaghetty_batch_destroy(b);
         return SPAGHETTY_ERR_CUDA;
     }
-    if ((size_t)b->smem_elems * sizeof(double) > 48 * 1024) {
+    if (batch_smem_bytes(b->smem_elems) > 48 * 1024) {
         if (cudaFuncSetAttribute(spg_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 b->smem_elems * (int)sizeof(double)) != cudaSuccess) {
+                                 (int)batch_smem_bytes(b->smem_elems)) != cudaSuccess) {
             cudaGetLastError();
             spaghetty_batch_destroy(b);
             return SPAGHETTY_ERR_CUDA;
@@ -298,7 +404,7 @@ int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
     void *args[] = {(void *)&jobs, (void *)&nj, (void *)&uj, (void *)&tu,
                     (void *)&counter, (void *)&status, (void *)&se};
     if (cudaLaunchKernel((const void *)spg_batched, dim3(grid), dim3(SPG_BATCH_NT), args,
-                         (size_t)b->smem_elems * sizeof(double), st) != cudaSuccess) {
+                         batch_smem_bytes(b->smem_elems), st) != cudaSuccess) {
         cudaGetLastError();
         return SPAGHETTY_ERR_CUDA;
     }
@@ -338,7 +444,7 @@ int spaghetty_batch_info(const spaghetty_batch *b, int64_t *info) {
     info[0] = b->njobs;
     info[1] = b->total_units;
     info[2] = b->bytes;
-    info[3] = b->smem_elems * (int64_t)sizeof(double);
+    info[3] = (int64_t)batch_smem_bytes(b->smem_elems);
     return SPAGHETTY_OK;
 }
 
@@ -459,7 +565,7 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
         j.ubeg = nunits;
         nunits += (pl.kp.ntiles + j.chunk - 1) / j.chunk;
         if (pl.kind == KIND_TILED)
-            smem_elems = std::max(smem_elems, pl.kp.vol + (pl.kp.pad ? pl.kp.vol / pl.kp.pad + 1 : 0));
+            smem_elems = std::max(smem_elems, (int)pl.kp.stage);
         ++njobs;
     }
     // the unit map follows the job records
@@ -497,7 +603,7 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
         cudaGetLastError();
         return SPAGHETTY_ERR_CUDA;
     }
-    const size_t smem = (size_t)smem_elems * sizeof(double);
+    const size_t smem = batch_smem_bytes(smem_elems);
     if (smem > 48 * 1024 &&
         cudaFuncSetAttribute(spg_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         cudaGetLastError();

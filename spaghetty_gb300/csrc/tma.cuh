@@ -12,15 +12,16 @@
 // into the output tile by the same bulk load.
 //
 // Pipeline (warp-specialised): S load stages, each an input tile,
-// (sortacc) an old-output tile and a "full" mbarrier, and two output slots,
-// each with a "done" mbarrier (the permute threads finished the box) and a
-// "free" mbarrier (the store has read the slot).  One producer thread keeps
-// every load stage busy and issues the stores; the permute threads never
-// meet at a block barrier inside the loop.  A load stage is refilled only
-// after every permute thread has consumed it, and an output slot is
-// rewritten only after the store issued two boxes earlier has read it.
-// Every wait is bounded: on timeout a thread records an error in the status
-// word and leaves; the producer waits (bounded) for its transfers in flight.
+// (sortacc) an old-output tile, a "full" mbarrier (the loads landed) and an
+// "empty" mbarrier (every permute warp has read it), and two output slots,
+// each with a "done" mbarrier (the permute warps wrote it) and a "free"
+// mbarrier (the store has read it).  One load thread keeps every stage
+// busy, one store thread issues the stores and waits for them to read their
+// slot, so a store never delays a refill; the permute threads never meet at a
+// block barrier inside the loop.  Every wait is bounded: on timeout a thread
+// records an error in the status word and leaves, and the load and store
+// threads wait (bounded) for their own transfers in flight before the CTA
+// retires.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -109,9 +110,9 @@ __device__ __forceinline__ void spg_mbar_arrive(uint32_t addr) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(addr) : "memory");
 }
 
-// Threads in one CTA of spg_tiled_tma: NT permute threads and one producer
-// warp.
-#define SPG_TMA_BLOCK(NT) ((NT) + 32)
+// Threads in one CTA of spg_tiled_tma: NT permute threads, one load warp and
+// one store warp (one active thread each).
+#define SPG_TMA_BLOCK(NT) ((NT) + 64)
 
 template <int NT, int EPT, int OP, int S>
 __global__ void __launch_bounds__(SPG_TMA_BLOCK(NT))
@@ -121,8 +122,8 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     extern __shared__ __align__(1024) unsigned char smem_raw0[];
     // load stage s at s*stage_bytes (input tile, then the old-output tile
     // for sortacc at +in_bytes); output slot o at S*stage_bytes +
-    // o*out_bytes; then the mbarriers: full[S], done[2], free[2].  The base
-    // is rounded up to 1024 bytes (the launch adds 1 KB).
+    // o*out_bytes; then the mbarriers: full[S], empty[S], done[2], free[2].
+    // The base is rounded up to 1024 bytes (the launch adds 1 KB).
     const uint32_t raw = (uint32_t)__cvta_generic_to_shared(smem_raw0);
     const uint32_t base = (raw + 1023u) & ~1023u;
     unsigned char *smem_raw = smem_raw0 + (base - raw);
@@ -131,10 +132,12 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     const uint32_t ob = (uint32_t)tp.out_bytes;
     const uint32_t out0 = (uint32_t)S * sb;
     const uint32_t full0 = base + out0 + 2u * ob;        // loads of a stage landed
-    const uint32_t done0 = full0 + 8u * S;               // permute threads finished a box
-    const uint32_t free0 = done0 + 16u;                  // store finished reading a slot
+    const uint32_t empty0 = full0 + 8u * S;              // permute threads read a stage
+    const uint32_t done0 = empty0 + 8u * S;              // permute threads wrote a slot
+    const uint32_t free0 = done0 + 16u;                  // the store has read a slot
     const uint32_t tid = threadIdx.x;
     const uint32_t G = gridDim.x;
+    const uint32_t load_tid = NT, store_tid = NT + 32;
 
     auto issue = [&](uint32_t t, int s) {
         int32_t ci[5], co[5];
@@ -145,13 +148,16 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
         if (spg_reads_out<OP>::value) spg_tma_load5(base + (uint32_t)s * sb + in_bytes, &tmap_out, co, mb);
         (void)co;
     };
-    // the producer thread sets up the barriers and fills every stage before
-    // the permute threads build their tables, so DRAM latency overlaps the
+    // the load thread sets up the barriers and fills every stage before the
+    // permute threads build their tables, so DRAM latency overlaps the
     // prologue
-    int issued = 0;                         // producer: boxes whose loads were issued
-    if (tid == NT) {
+    int issued = 0;                         // load thread: boxes whose loads were issued
+    if (tid == load_tid) {
 #pragma unroll
-        for (int s = 0; s < S; ++s) spg_mbar_init(full0 + 8u * s, 1u);
+        for (int s = 0; s < S; ++s) {
+            spg_mbar_init(full0 + 8u * s, 1u);
+            spg_mbar_init(empty0 + 8u * s, (uint32_t)(NT / 32));
+        }
 #pragma unroll
         for (int o = 0; o < 2; ++o) {
             spg_mbar_init(done0 + 8u * o, (uint32_t)(NT / 32));
@@ -179,39 +185,45 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     }
     __syncthreads();                        // barriers initialised before anyone waits
 
-    if (tid >= NT) {
-        // ---- producer: one thread issues every bulk copy ----
-        if (tid != NT) return;
-        int it = 0;
+    if (tid == load_tid) {
+        // ---- loads: refill stage s with box it+S once box it has been read ----
         bool ok = true;
-        for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
+        int it = 0;
+        for (uint32_t t = blockIdx.x + (uint32_t)S * G; t < p.ntiles; t += G, ++it) {
             const int s = it % S;
+            ok = spg_mbar_wait(empty0 + 8u * (uint32_t)s, (uint32_t)((it / S) & 1));
+            if (!ok) break;
+            issue(t, s);
+            ++issued;
+        }
+        if (!ok && tp.status) *(volatile int *)tp.status = 1;
+        // the CTA must not retire with a load in flight: wait (bounded) for
+        // the last S issued, which on the normal path have already landed
+        for (int j = issued > S ? issued - S : 0; j < issued; ++j)
+            spg_mbar_wait(full0 + 8u * (uint32_t)(j % S), (uint32_t)((j / S) & 1));
+        return;
+    }
+    if (tid == store_tid) {
+        // ---- stores: box it from slot it&1 once the permute threads wrote it ----
+        bool ok = true;
+        int it = 0;
+        for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
             const int o = it & 1;
-            // the permute threads have read stage s and written slot o
             ok = spg_mbar_wait(done0 + 8u * (uint32_t)o, (uint32_t)((it >> 1) & 1));
             if (!ok) break;
             int32_t ci[5], co[5];
             spg_tma_coords(p, tp, t, ci, co);
             spg_tma_store5(&tmap_out, co, base + out0 + (uint32_t)o * ob);
             spg_bulk_commit();
-            const uint32_t tn = t + (uint32_t)S * G;
-            if (tn < p.ntiles) { issue(tn, s); ++issued; }
             // slot o is free again once this store has read it
             spg_bulk_wait_read<0>();
             spg_mbar_arrive(free0 + 8u * (uint32_t)o);
         }
+        if (!ok && tp.status) *(volatile int *)tp.status = 1;
         spg_bulk_wait0();                   // stores complete before the CTA retires
-        if (!ok) {
-            if (tp.status) *(volatile int *)tp.status = 1;
-            // bounded wait for the loads still in flight (boxes it..issued-1)
-            for (int j = it; j < issued; ++j) {
-                const uint32_t mb = full0 + 8u * (uint32_t)(j % S);
-                for (uint32_t i = 0; i < 4096u && !spg_mbar_try_wait(mb, (uint32_t)((j / S) & 1)); ++i) {
-                }
-            }
-        }
         return;
     }
+    if (tid >= NT) return;                  // idle lanes of the load and store warps
 
     // ---- permute threads ----
     const SpgFactor fac = p.fac;
@@ -242,6 +254,9 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
         }
         spg_fence_async_smem();             // generic-proxy writes -> visible to the bulk store
         __syncwarp();
-        if (lane == 0) spg_mbar_arrive(done0 + 8u * (uint32_t)o);
+        if (lane == 0) {
+            spg_mbar_arrive(empty0 + 8u * (uint32_t)s);
+            spg_mbar_arrive(done0 + 8u * (uint32_t)o);
+        }
     }
 }
