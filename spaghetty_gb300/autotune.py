@@ -251,8 +251,9 @@ def apply_cache(cache: dict | None = None, gpu: str | None = None) -> int:
     return nset
 
 
-def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False):
-    """Time every candidate for (dims, perm, op); store and apply the best."""
+def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False, dump=None):
+    """Time every candidate for (dims, perm, op); store and apply the best.
+    ``dump``: an open text file that receives every candidate's time."""
     import torch
     p, cands = candidates(dims, perm, op)
     if not cands:
@@ -279,6 +280,13 @@ def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False):
         except Exception:
             continue
         results.append((t, cfg))
+        if dump is not None:
+            dump.write(json.dumps({"dims": list(dims), "perm": list(perm), "op": op, "box": cfg[0],
+                                   "threads": cfg[1], "ept": cfg[2], "stages": cfg[3],
+                                   "seconds": t}) + "\n")
+    if dump is not None:
+        dump.write(json.dumps({"dims": list(dims), "perm": list(perm), "op": op, "default": True,
+                               "seconds": t_default}) + "\n")
     clear()
     if not results:
         return None
@@ -315,6 +323,7 @@ def main():
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--cache", default=DEFAULT_CACHE)
     ap.add_argument("--force", action="store_true")
+    ap.add_argument("--dump", default=None, help="write every candidate's time to this file")
     args = ap.parse_args()
     from .workloads import PERMS4, SORT4_DIMS, TRIPLES_SORT6
     ops = [int(x) for x in args.ops.split(",")]
@@ -334,11 +343,14 @@ def main():
         probs = [(tuple(int(x) for x in args.dims.split(",")),
                   tuple(int(x) for x in args.perm.split(",")))]
     cache = load_cache(args.cache)
+    dump = open(args.dump, "w") if args.dump else None
     t0 = time.time()
     for dims, perm in probs:
         for op in ops:
-            tune(dims, perm, op, args.reps, cache, verbose=True, force=args.force)
+            tune(dims, perm, op, args.reps, cache, verbose=True, force=args.force, dump=dump)
         save_cache(cache, args.cache)
+    if dump is not None:
+        dump.close()
     print("tuned %d problems in %.1fs" % (len(probs) * len(ops), time.time() - t0))
 
 
