@@ -30,12 +30,7 @@
 #define SPG_BATCH_EPT 4
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
 #define SPG_BATCH_UNIT_ELEMS 16384
-#ifndef SPG_BATCH_S
-#define SPG_BATCH_S 3          // cp.async stages of the tiled path
-#endif
-#ifndef SPG_BATCH_DIRECT2
-#define SPG_BATCH_DIRECT2 1    // direct sorts: two boxes in flight per step
-#endif
+#define SPG_BATCH_S 4          // cp.async stages of the tiled path
 
 struct BatchJob {
     KParams kp;
@@ -119,45 +114,13 @@ __device__ __forceinline__ void spg_batch_tiled(const BatchJob &j, const SpgTab<
     spg_cp_wait<0>();
 }
 
-// Boxes [b0, b1) of one direct sort, two boxes per step so that twice the
-// loads are in flight.
-template <int OP>
-__device__ __forceinline__ void spg_batch_direct(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
-                                                 uint32_t b0, uint32_t b1) {
-    const KParams &p = j.kp;
-    const SpgFactor fac = p.fac;
-    uint32_t t = b0;
-    for (; SPG_BATCH_DIRECT2 && t + 1 < b1; t += 2) {
-        int64_t ib[2], ob[2];
-        uint32_t lA[2], lB[2];
-        spg_box(p, t, ib[0], ob[0], lA[0], lB[0]);
-        spg_box(p, t + 1, ib[1], ob[1], lA[1], lB[1]);
-        double v[2][SPG_BATCH_EPT], y[2][SPG_BATCH_EPT];
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-#pragma unroll
-            for (int k = 0; k < SPG_BATCH_EPT; ++k) {
-                v[h][k] = 0.0; y[h][k] = 0.0;
-                if (spg_valid(tb.pkl[k], lA[h], lB[h])) {
-                    v[h][k] = spg_ld_in(j.in + ib[h] + tb.ioff[k]);
-                    if (spg_reads_out<OP>::value) y[h][k] = spg_ld_out(j.out + ob[h] + tb.ooff[k]);
-                }
-            }
-#pragma unroll
-        for (int h = 0; h < 2; ++h)
-#pragma unroll
-            for (int k = 0; k < SPG_BATCH_EPT; ++k)
-                if (spg_valid(tb.pkl[k], lA[h], lB[h]))
-                    spg_st_out(j.out + ob[h] + tb.ooff[k], spg_apply<OP>(v[h][k], y[h][k], fac));
-    }
-    if (t < b1) spg_direct_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(p, tb, j.in, j.out, t);
-}
-
 template <int OP>
 __device__ __forceinline__ void spg_batch_units(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
                                                 uint32_t b0, uint32_t b1, double *sm) {
     if (j.kind == KIND_TILED) spg_batch_tiled<OP>(j, tb, b0, b1, sm);
-    else spg_batch_direct<OP>(j, tb, b0, b1);
+    else
+        for (uint32_t t = b0; t < b1; ++t)
+            spg_direct_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(j.kp, tb, j.in, j.out, t);
 }
 
 __global__ void __launch_bounds__(SPG_BATCH_NT)
