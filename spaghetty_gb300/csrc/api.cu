@@ -222,7 +222,7 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         // permute step
         int box[SPG_MAXR];
         Plan tp;
-        if (spg_default_box_tma(fo, sms, box) == SPAGHETTY_OK &&
+        if (spg_default_box_tma(fo, sms, 2048, box) == SPAGHETTY_OK &&
             spg_plan(fo, op, box, 256, 8, 0, sms, &tp) == SPAGHETTY_OK &&
             spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_TILED &&
             tp.wf_pad0 <= 2 * tp.wf_ideal) {
@@ -236,6 +236,17 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
                 if (to_tma(&tp, 256, 8, stages, false) == SPAGHETTY_OK) *pl = tp;
             }
         }
+    } else if (pl->kind == KIND_DIRECT && allow_tma) {
+        // the stride-1 index stays put: the same-order TMA plan (no
+        // transposition in shared memory) with a box of at most 1K
+        // elements, 128 threads x 8, 2 load stages
+        int box[SPG_MAXR];
+        Plan tp;
+        if (spg_default_box_tma(fo, sms, 1024, box) == SPAGHETTY_OK &&
+            spg_plan(fo, op, box, 128, 8, 0, sms, &tp) == SPAGHETTY_OK &&
+            spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_DIRECT &&
+            to_tma(&tp, 128, 8, 2, false) == SPAGHETTY_OK)
+            *pl = tp;
     }
     return SPAGHETTY_OK;
 }

@@ -334,7 +334,7 @@ int spg_plan(const Folded &fo, int op, const int *box_override, int threads_over
 // Default box for the TMA-staged kernel: smaller than the register-staged
 // kernels' (boxes of ~1-2K elements keep 3-4 CTAs and their pipelines
 // resident per SM), with the same >= 32-double runs on both sides.
-int spg_default_box_tma(const Folded &fo, int num_sms, int *box) {
+int spg_default_box_tma(const Folded &fo, int num_sms, int vmax, int *box) {
     if (fo.empty || fo.rank < 2) return SPAGHETTY_ERR_CONFIG;
     const int R = fo.rank;
     Shape s;
@@ -342,14 +342,14 @@ int spg_default_box_tma(const Folded &fo, int num_sms, int *box) {
     for (int d = 0; d < R; ++d) { s.D[d] = fo.D[d]; s.in_order[d] = R - 1 - d; }
     for (int q = 0; q < R; ++q) s.out_order[q] = fo.P[R - 1 - q];
     int64_t L[SPG_MAXR];
-    choose_box(s, std::min<int64_t>(fo.nelem, (int64_t)1024 * 4 * std::max(1, num_sms)), num_sms, L, 2048);
+    choose_box(s, std::min<int64_t>(fo.nelem, (int64_t)1024 * 4 * std::max(1, num_sms)), num_sms, L, vmax);
     // the bulk copy's innermost box row must be a multiple of 16 bytes
     if (L[R - 1] % 2 && L[R - 1] < s.D[R - 1]) L[R - 1] += 1;
     const int ob = fo.P[R - 1];
     if (L[ob] % 2 && L[ob] < s.D[ob]) L[ob] += 1;
     int64_t vol = 1;
     for (int d = 0; d < R; ++d) vol *= L[d];
-    if (vol > 2048) return SPAGHETTY_ERR_CONFIG;
+    if (vol > vmax) return SPAGHETTY_ERR_CONFIG;
     for (int d = 0; d < R; ++d) box[d] = (int)L[d];
     return SPAGHETTY_OK;
 }

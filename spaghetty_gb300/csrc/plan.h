@@ -160,7 +160,7 @@ int spg_choose_op(double f, double g);
 int spg_plan(const Folded &fo, int op, const int *box_override, int threads_override,
              int ept_override, int stages_override, int num_sms, Plan *out);
 int spg_plan_batch(const Folded &fo, int op, Plan *out);
-int spg_default_box_tma(const Folded &fo, int num_sms, int *box);
+int spg_default_box_tma(const Folded &fo, int num_sms, int vmax, int *box);
 int spg_build_params(Plan *pl, double f, double g);
 SpgFactor spg_make_factor(double f, double g);
 int spg_selftest_host(void);
