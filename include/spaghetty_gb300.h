@@ -354,6 +354,15 @@ int spaghetty_batch_poison(spaghetty_batch *batch, int index);
 
 int spaghetty_batch_destroy(spaghetty_batch *batch);
 
+/* Autotuner hook of the batched kernel (per-size-bucket tile shapes): sorts
+ * of rank `rank` whose largest extent lies in [ext_lo, ext_hi] get boxes
+ * grown until the input and output rows hold run_in / run_out contiguous
+ * doubles, towards `volume` elements (at most 1024).  A bucket overlapping
+ * an existing one replaces it; rank 0 clears every rule.  Applies to batches
+ * created afterwards.  The tune file's `batch` lines install these rules.
+ * Returns a SPAGHETTY_* code. */
+int spaghetty_batch_tune_set(int rank, int ext_lo, int ext_hi, int run_in, int run_out, int volume);
+
 /* Batched sorts for callers that cannot allocate device memory -- code
  * running while a CUDA graph is being captured (where cudaMalloc is not
  * allowed), or inside an application that owns the whole device memory

@@ -227,6 +227,12 @@ def save_cache(cache: dict, path=DEFAULT_CACHE):
     for gk, ents in sorted(cache.items()):
         name, sms = gk.rsplit("/", 1)
         for key, e in sorted(ents.items()):
+            if key.startswith("batch|"):
+                if e.get("rule"):
+                    _, rank, lo, hi = key.split("|")
+                    lines.append("|".join([name, sms.rstrip("sm"), "batch", rank, lo, hi]
+                                          + [str(v) for v in e["rule"]]))
+                continue
             d, p, cls = key.split("|")
             lines.append("|".join([name, sms.rstrip("sm"), d, p, cls,
                                    ",".join(map(str, e["box"])), str(e["threads"]),
@@ -242,6 +248,11 @@ def apply_cache(cache: dict | None = None, gpu: str | None = None) -> int:
     gpu = gpu or gpu_key()
     nset = 0
     for key, ent in cache.get(gpu, {}).items():
+        if key.startswith("batch|"):
+            if ent.get("rule"):
+                _, rank, lo, hi = key.split("|")
+                nset += lib().spaghetty_batch_tune_set(int(rank), int(lo), int(hi), *ent["rule"]) == 0
+            continue
         dims_s, perm_s, cls = key.split("|")
         D = [int(x) for x in dims_s.split(",")]
         # the folded problem itself is a valid (dims, perm) call: perm 1-based
@@ -313,10 +324,108 @@ def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False, dump=
     return ent
 
 
+# Size buckets of the batched kernel (rank -> inclusive ranges of the largest
+# extent) and the candidate tile-shape rules (input run, output run, volume).
+BATCH_BUCKETS = {4: [(1, 11), (12, 19), (20, 27), (28, 64)], 6: [(1, 8), (9, 12), (13, 16), (17, 32)]}
+BATCH_RULES = [(ti, to, vt) for ti in (8, 16, 32, 64) for to in (8, 16, 32, 64)
+               for vt in (256, 512, 1024)]
+
+
+def _batch_rules_except(cache, gk, skip):
+    """Clear every bucket rule, then install the cached winners but `skip`."""
+    lib().spaghetty_batch_tune_set(0, 0, 0, 0, 0, 0)
+    for key, ent in cache.get(gk, {}).items():
+        if key.startswith("batch|") and key != skip and ent.get("rule"):
+            _, rank, lo, hi = key.split("|")
+            lib().spaghetty_batch_tune_set(int(rank), int(lo), int(hi), *ent["rule"])
+
+
+def tune_batched(cache, n=4096, seed=2024, budget_bytes=6 << 30, reps=3, verbose=True, force=False,
+                 dump=None):
+    """Per-size-bucket tile shapes of the persistent batched kernel, tuned on
+    the batched configuration's own mix (workloads.batched_mix): for each
+    bucket, the jobs of the mix that fall in it (up to budget_bytes) run as
+    one batch under every candidate rule; the fastest rule is kept, or none
+    when the built-in planner is faster."""
+    import torch
+    from .batched import Batch
+    from .workloads import batched_mix
+    dev = torch.device("cuda", torch.cuda.current_device())
+    gk = gpu_key()
+    mix = batched_mix(n, seed=seed)
+    flush = torch.empty((512 << 20) // 4, dtype=torch.float32, device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(seed)
+
+    def timed(jobs):
+        b = Batch(jobs)
+        try:
+            ts = []
+            for r in range(reps + 1):
+                flush.fill_(1.0)
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record()
+                b.launch()
+                e1.record()
+                e1.synchronize()
+                if r:
+                    ts.append(e0.elapsed_time(e1) / 1e3)
+            if b.status() != 0:
+                raise RuntimeError("batched status word set")
+        finally:
+            b.close()
+        ts.sort()
+        return ts[len(ts) // 2]
+
+    for rank, buckets in BATCH_BUCKETS.items():
+        for lo, hi in buckets:
+            key = "batch|%d|%d|%d" % (rank, lo, hi)
+            if not force and key in cache.get(gk, {}):
+                continue
+            jobs, used = [], 0
+            for m in mix:
+                if len(m["dims"]) != rank or not (lo <= max(m["dims"]) <= hi):
+                    continue
+                k = 1
+                for d in m["dims"]:
+                    k *= d
+                if used + 16 * k > budget_bytes:
+                    continue
+                u = torch.rand(k, dtype=torch.float64, device=dev, generator=gen) - 0.5
+                sb = torch.rand(k, dtype=torch.float64, device=dev, generator=gen) - 0.5
+                jobs.append((u, sb, m["dims"], m["perm"], m["factor"], 1.0 if m["acc"] else 0.0))
+                used += 16 * k
+            if not jobs:
+                continue
+            _batch_rules_except(cache, gk, key)
+            t_default = timed(jobs)
+            results = []
+            for rule in BATCH_RULES:
+                if lib().spaghetty_batch_tune_set(rank, lo, hi, *rule) != 0:
+                    continue
+                t = timed(jobs)
+                results.append((t, rule))
+                if dump is not None:
+                    dump.write(json.dumps({"batch": [rank, lo, hi], "rule": rule, "seconds": t}) + "\n")
+            _batch_rules_except(cache, gk, key)
+            results.sort()
+            t, rule = results[0]
+            ent = {"rule": list(rule) if t < t_default else None, "seconds": min(t, t_default),
+                   "default_seconds": t_default, "jobs": len(jobs), "bytes": used,
+                   "gbs": used / min(t, t_default) / 1e9, "default_gbs": used / t_default / 1e9}
+            cache.setdefault(gk, {})[key] = ent
+            if verbose:
+                print(json.dumps({"bucket": key, **ent}), flush=True)
+            del jobs
+            torch.cuda.empty_cache()
+    apply_cache(cache, gk)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--sweep", default="sort4",
-                    choices=["sort4", "sort6-triples", "sort6-sample", "case"])
+                    choices=["sort4", "sort6-triples", "sort6-sample", "batched", "case"])
     ap.add_argument("--dims", default="100,100,100,100")
     ap.add_argument("--perm", default="4,3,2,1")
     ap.add_argument("--ops", default="0,1")
@@ -344,6 +453,14 @@ def main():
                   tuple(int(x) for x in args.perm.split(",")))]
     cache = load_cache(args.cache)
     dump = open(args.dump, "w") if args.dump else None
+    if args.sweep == "batched":
+        t0 = time.time()
+        tune_batched(cache, reps=args.reps, force=args.force, dump=dump)
+        save_cache(cache, args.cache)
+        if dump is not None:
+            dump.close()
+        print("tuned the batched buckets in %.1fs" % (time.time() - t0))
+        return
     t0 = time.time()
     for dims, perm in probs:
         for op in ops:

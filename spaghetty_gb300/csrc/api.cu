@@ -632,7 +632,9 @@ int call_r(const char *who, bool print, int rank, const double *u, double *s, co
 
 // Tune file: one winner per line,
 //   gpu_name|sm_count|D0,D1,..|P0,P1,..|op_class|box0,box1,..|threads|ept|stages
-// (folded dims and 0-based folded permutation, as the autotuner writes them).
+// (folded dims and 0-based folded permutation, as the autotuner writes them),
+// and one line per size bucket of the batched kernel,
+//   gpu_name|sm_count|batch|rank|ext_lo|ext_hi|run_in|run_out|volume
 int load_tune_file(const char *path, bool only_this_gpu) {
     FILE *fh = std::fopen(path, "r");
     if (!fh) return -1;
@@ -661,6 +663,13 @@ int load_tune_file(const char *path, bool only_this_gpu) {
         if (nf != 9) continue;
         if (only_this_gpu && (!have_dev || std::strcmp(fields[0], name) != 0 || std::atoi(fields[1]) != sms))
             continue;
+        if (std::strcmp(fields[2], "batch") == 0) {
+            if (spaghetty_batch_tune_set(std::atoi(fields[3]), std::atoi(fields[4]), std::atoi(fields[5]),
+                                         std::atoi(fields[6]), std::atoi(fields[7]),
+                                         std::atoi(fields[8])) == SPAGHETTY_OK)
+                ++installed;
+            continue;
+        }
         int D[SPG_MAXR], P[SPG_MAXR], B[SPG_MAXR];
         auto parse = [](char *txt, int *out) {
             int n = 0;
@@ -702,6 +711,10 @@ void autoload_tune_file() {
 }
 
 }  // namespace
+
+// Installs the tune file beside the library once per process (batch.cu calls
+// it before planning a batch, so that its size-bucket rules apply).
+void spg_autoload_tune() { autoload_tune_file(); }
 
 // ===========================================================================
 extern "C" {

@@ -47,6 +47,10 @@ struct BatchJob {
 static inline size_t batch_smem_bytes(int stage_elems) {
     return (size_t)SPG_BATCH_S * (size_t)stage_elems * sizeof(double);
 }
+// The kernel also holds the current job record in static shared memory, and
+// the 48 KB default limit counts static plus dynamic bytes: above this many
+// dynamic bytes the launch needs the opt-in attribute.
+#define SPG_BATCH_SMEM_OPTIN (40 * 1024)
 
 // Status word bits.
 #define SPG_ST_BAD_JOB 1
@@ -211,6 +215,23 @@ struct spaghetty_batch {
 namespace {
 thread_local int g_batch_bad_index = -1;
 
+// Tuned tile-shape rules, one per size bucket (spaghetty_batch_tune_set).
+std::mutex g_rules_mu;
+std::vector<SpgBatchRule> g_rules;
+
+// The rule for one sort: its rank and its largest extent pick the bucket.
+bool find_rule(int rank, const int *dims, SpgBatchRule *out) {
+    int emax = 0;
+    for (int q = 0; q < rank; ++q) emax = std::max(emax, dims[q]);
+    std::lock_guard<std::mutex> lk(g_rules_mu);
+    for (const SpgBatchRule &r : g_rules)
+        if (r.rank == rank && emax >= r.ext_lo && emax <= r.ext_hi) {
+            *out = r;
+            return true;
+        }
+    return false;
+}
+
 bool is_device_ptr(const void *p, int *dev) {
     cudaPointerAttributes at;
     std::memset(&at, 0, sizeof(at));
@@ -254,6 +275,7 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         delete b;
         return SPAGHETTY_ERR_CUDA;
     }
+    spg_autoload_tune();                      // size-bucket rules from the tune file
     std::vector<uint32_t> unit_job;
     struct Range { uintptr_t lo, hi; int idx; bool out; };
     std::vector<Range> ranges;
@@ -277,7 +299,9 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         ranges.push_back({(uintptr_t)e.sorted, (uintptr_t)e.sorted + nb, i, true});
         Plan pl;
         const int op = spg_choose_op(e.factor, e.acc_factor);
-        rc = spg_plan_batch(fo, op, &pl);
+        SpgBatchRule rule;
+        const bool have_rule = find_rule(e.rank, e.dims, &rule);
+        rc = spg_plan_batch(fo, op, have_rule ? &rule : nullptr, &pl);
         if (!rc) rc = spg_build_params(&pl, e.factor, e.acc_factor);
         if (rc) { g_batch_bad_index = i; break; }
         BatchJob j;
@@ -335,7 +359,7 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         spaghetty_batch_destroy(b);
         return SPAGHETTY_ERR_CUDA;
     }
-    if (batch_smem_bytes(b->smem_elems) > 48 * 1024) {
+    if (batch_smem_bytes(b->smem_elems) > SPG_BATCH_SMEM_OPTIN) {
         if (cudaFuncSetAttribute(spg_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)batch_smem_bytes(b->smem_elems)) != cudaSuccess) {
             cudaGetLastError();
@@ -348,6 +372,25 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
 }
 
 int spaghetty_batch_bad_index(void) { return g_batch_bad_index; }
+
+int spaghetty_batch_tune_set(int rank, int ext_lo, int ext_hi, int run_in, int run_out, int volume) {
+    std::lock_guard<std::mutex> lk(g_rules_mu);
+    if (rank == 0) {
+        g_rules.clear();
+        return SPAGHETTY_OK;
+    }
+    if (rank < 1 || rank > SPG_MAXR || ext_lo < 1 || ext_hi < ext_lo || run_in < 1 || run_out < 1 ||
+        volume < 1 || volume > SPG_BATCH_VMAX)
+        return SPAGHETTY_ERR_CONFIG;
+    // a bucket overlapping an existing one replaces it
+    for (size_t q = 0; q < g_rules.size();) {
+        const SpgBatchRule &r = g_rules[q];
+        if (r.rank == rank && !(ext_hi < r.ext_lo || r.ext_hi < ext_lo)) g_rules.erase(g_rules.begin() + q);
+        else ++q;
+    }
+    g_rules.push_back({rank, ext_lo, ext_hi, run_in, run_out, volume});
+    return SPAGHETTY_OK;
+}
 
 int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
     if (!b) return SPAGHETTY_ERR_NULL;
@@ -510,7 +553,9 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
         }
         Plan pl;
         const int op = spg_choose_op(e.factor, e.acc_factor);
-        rc = spg_plan_batch(fo, op, &pl);
+        SpgBatchRule rule;
+        const bool have_rule = find_rule(e.rank, e.dims, &rule);
+        rc = spg_plan_batch(fo, op, have_rule ? &rule : nullptr, &pl);
         if (!rc) rc = spg_build_params(&pl, e.factor, e.acc_factor);
         if (rc) { g_batch_bad_index = i; return rc; }
         const uintptr_t nb = (uintptr_t)fo.nelem * sizeof(double);
@@ -567,7 +612,7 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
         return SPAGHETTY_ERR_CUDA;
     }
     const size_t smem = batch_smem_bytes(smem_elems);
-    if (smem > 48 * 1024 &&
+    if (smem > SPG_BATCH_SMEM_OPTIN &&
         cudaFuncSetAttribute(spg_batched, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
         cudaGetLastError();
         return SPAGHETTY_ERR_CUDA;

@@ -179,18 +179,23 @@ static const int kDefaultStages = 3;
 static const int kBatchThreads = 256;
 static const int kBatchEpt = 4;
 
-static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L, int vmax) {
+// Greedy box: grow the box until the input rows hold trun_in and the output
+// rows trun_out contiguous doubles (or the whole extent of that side), then
+// towards a target volume: vtarget when positive, else one that still leaves
+// a few boxes per SM.
+static void choose_box_t(const Shape &s, int64_t nelem, int num_sms, int64_t *L, int vmax,
+                         int trun_in, int trun_out, int vtarget) {
     for (int d = 0; d < s.R; ++d) L[d] = 1;
-    // phase 1: both runs >= kTRun (or the whole extent of that side)
+    // phase 1: both runs long enough
     for (int it = 0; it < 64; ++it) {
         int64_t vol = volume(s, L);
         int64_t ri = run_len(s, L, s.in_order), ro = run_len(s, L, s.out_order);
         int d = -1;
         int64_t need = 0;
-        if (ri < kTRun && (d = frontier(s, L, s.in_order)) >= 0) {
-            need = (kTRun * L[d] + ri - 1) / ri;
-        } else if (ro < kTRun && (d = frontier(s, L, s.out_order)) >= 0) {
-            need = (kTRun * L[d] + ro - 1) / ro;
+        if (ri < trun_in && (d = frontier(s, L, s.in_order)) >= 0) {
+            need = (trun_in * L[d] + ri - 1) / ri;
+        } else if (ro < trun_out && (d = frontier(s, L, s.out_order)) >= 0) {
+            need = (trun_out * L[d] + ro - 1) / ro;
         } else {
             break;
         }
@@ -203,6 +208,7 @@ static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L, i
     // enough boxes to fill every SM a few times
     int64_t target = nelem / (4 * (int64_t)std::max(1, num_sms));
     target = std::max<int64_t>(256, std::min<int64_t>(2048, target));
+    if (vtarget > 0) target = vtarget;
     for (int it = 0; it < 64; ++it) {
         int64_t vol = volume(s, L);
         if (vol >= target) break;
@@ -225,6 +231,10 @@ static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L, i
     for (int d = 0; d < s.R; ++d)
         if (L[d] < s.D[d] && s.D[d] % L[d] != 0 && d != fi && d != fo)
             L[d] = largest_divisor_le(s.D[d], L[d]);
+}
+
+static void choose_box(const Shape &s, int64_t nelem, int num_sms, int64_t *L, int vmax) {
+    choose_box_t(s, nelem, num_sms, L, vmax, kTRun, kTRun, 0);
 }
 
 static int pick_block(int vol, int *threads, int *ept) {
@@ -357,7 +367,7 @@ int spg_default_box_tma(const Folded &fo, int num_sms, int vmax, int *box) {
 // Plan for one sort of a batch: the persistent batched kernel runs every
 // sort with one CTA shape (256 threads x 8 elements), so boxes are capped at
 // 2048 elements, and a rank <= 1 problem becomes a 1-D direct box.
-int spg_plan_batch(const Folded &fo, int op, Plan *pl) {
+int spg_plan_batch(const Folded &fo, int op, const SpgBatchRule *rule, Plan *pl) {
     std::memset(pl, 0, sizeof(*pl));
     pl->fo = fo;
     pl->op = op;
@@ -381,8 +391,13 @@ int spg_plan_batch(const Folded &fo, int op, Plan *pl) {
     for (int d = 0; d < R; ++d) { s.D[d] = fo.D[d]; s.in_order[d] = R - 1 - d; }
     for (int q = 0; q < R; ++q) s.out_order[q] = fo.P[R - 1 - q];
     int64_t L[SPG_MAXR];
-    // many sorts share the GPU, so aim for full-size boxes
-    choose_box(s, (int64_t)1 << 40, 1, L, vmax);
+    // many sorts share the GPU, so aim for full-size boxes, unless a tuned
+    // rule for this size bucket says otherwise
+    if (rule)
+        choose_box_t(s, (int64_t)1 << 40, 1, L, vmax, rule->run_in, rule->run_out,
+                     std::min(rule->volume, vmax));
+    else
+        choose_box(s, (int64_t)1 << 40, 1, L, vmax);
     for (int d = 0; d < R; ++d) pl->box[d] = (int)L[d];
     pl->run_in = (int)run_len(s, L, s.in_order);
     pl->run_out = (int)run_len(s, L, s.out_order);

@@ -159,7 +159,16 @@ int spg_fold(int rank, const int *dims, const int *perm, Folded *out);
 int spg_choose_op(double f, double g);
 int spg_plan(const Folded &fo, int op, const int *box_override, int threads_override,
              int ept_override, int stages_override, int num_sms, Plan *out);
-int spg_plan_batch(const Folded &fo, int op, Plan *out);
+// Tile-shape rule of the batched kernel for one size bucket: sorts of rank
+// `rank` whose largest extent lies in [ext_lo, ext_hi] get boxes grown until
+// the input and output rows hold run_in / run_out doubles, towards `volume`
+// elements.
+struct SpgBatchRule {
+    int rank, ext_lo, ext_hi, run_in, run_out, volume;
+};
+int spg_plan_batch(const Folded &fo, int op, const SpgBatchRule *rule, Plan *out);
+// Installs the tune file beside the library once per process (api.cu).
+void spg_autoload_tune();
 int spg_default_box_tma(const Folded &fo, int num_sms, int vmax, int *box);
 int spg_build_params(Plan *pl, double f, double g);
 SpgFactor spg_make_factor(double f, double g);

@@ -67,8 +67,9 @@ def verify(dims, perm, op=0, sms=152):
 ])
 def test_folding(dims, perm, rank, kind):
     p = plan(dims, perm)
-    # a tiled plan runs on the TMA-staged kernel when its boxes allow it
-    assert p["rank"] == rank and (p["kind"] == kind or (kind, p["kind"]) == ("tiled", "tma"))
+    # tiled and direct plans run on the TMA-staged kernel when its boxes
+    # allow it (direct ones with the same-order layout)
+    assert p["rank"] == rank and (p["kind"] == kind or (kind in ("tiled", "direct") and p["kind"] == "tma"))
     assert int(np.prod(p["dims"])) == int(np.prod(dims))
 
 
@@ -210,3 +211,14 @@ def test_tma_candidates_replay_rank4():
     finally:
         clear()
     assert same_order_seen > 0
+
+
+def test_batch_tune_set_validation():
+    L = lib()
+    assert L.spaghetty_batch_tune_set(4, 8, 16, 16, 32, 512) == 0
+    assert L.spaghetty_batch_tune_set(4, 12, 20, 8, 8, 256) == 0      # overlapping bucket replaces
+    assert L.spaghetty_batch_tune_set(4, 8, 16, 16, 32, 2048) == 9    # volume above 1024
+    assert L.spaghetty_batch_tune_set(9, 8, 16, 16, 32, 512) == 9     # rank
+    assert L.spaghetty_batch_tune_set(4, 16, 8, 16, 32, 512) == 9     # empty range
+    assert L.spaghetty_batch_tune_set(4, 8, 16, 0, 32, 512) == 9      # run
+    assert L.spaghetty_batch_tune_set(0, 0, 0, 0, 0, 0) == 0          # clear

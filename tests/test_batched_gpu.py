@@ -159,3 +159,27 @@ def test_mix_4096_reduced_extents(cuda):
     for i in rnd.sample(range(4096), 64):
         u, y, g = host[i]
         assert bits_equal(ja[i][1].cpu().numpy(), expect(specs[i], u, y, g)), i
+
+
+@pytest.mark.parametrize("rule", [(8, 8, 256), (64, 16, 1024), (16, 64, 512)])
+def test_size_bucket_rules(cuda, rule):
+    """Tuned per-size-bucket tile shapes (spaghetty_batch_tune_set) change
+    the boxes, never the bits."""
+    from spaghetty_gb300._lib import lib
+    from spaghetty_gb300.batched import Batch
+    L = lib()
+    specs = small_specs(96, 5)
+    jobs, host = make_jobs(specs, cuda, 300)
+    try:
+        assert L.spaghetty_batch_tune_set(4, 1, 64, *rule) == 0
+        assert L.spaghetty_batch_tune_set(6, 1, 64, *rule) == 0
+        b = Batch(jobs)
+        b.launch()
+        assert b.status() == 0
+        b.close()
+    finally:
+        L.spaghetty_batch_tune_set(0, 0, 0, 0, 0, 0)
+    for sp, (du, ds, *_), (u, y, g) in zip(specs, jobs, host):
+        got = ds.cpu().numpy()
+        want = expect(sp, u, y, g)
+        assert bits_equal(got, want), (sp, rule, first_mismatch(got, want))
