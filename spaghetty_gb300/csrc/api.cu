@@ -216,37 +216,55 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
     if (rc) return rc;
     rc = spg_build_params(pl, f, g);
     if (rc) return rc;
-    if (pl->kind == KIND_TILED && allow_tma) {
-        // default TMA plan: its own (smaller) box, 256 threads; kept only
-        // when its unpadded tile reads at most 2-way bank conflicts in the
-        // permute step
+    // Default plans, chosen from the GB300 autotuner's timings of every
+    // candidate over the sort4 sweep, the sort6 sample and random shapes:
+    //  - transposes: the TMA-staged kernel on the greedy box with 32-double
+    //    rows on both sides grown towards 4096 elements, the smallest CTA
+    //    (128x8, 256x8, 256x16) that holds it, 3 load stages (2 when 3 do
+    //    not fit); otherwise the register-staged tiled kernel on the greedy
+    //    box with 16/32-double rows towards 512 elements;
+    //  - the stride-1 index unchanged: the same-order TMA plan on a box of
+    //    at most 1K elements, 128 threads x 8, 3 load stages (else 2).
+    if (pl->kind == KIND_TILED) {
         int box[SPG_MAXR];
         Plan tp;
-        if (spg_default_box_tma(fo, sms, 2048, box) == SPAGHETTY_OK &&
-            spg_plan(fo, op, box, 256, 8, 0, sms, &tp) == SPAGHETTY_OK &&
-            spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_TILED &&
-            tp.wf_pad0 <= 2 * tp.wf_ideal) {
-            TmaLayout tl;
-            if (spg_tma_layout(tp, 4, &tl) == SPAGHETTY_OK) {
-                // the deepest of 4/3/2 load stages that still lets two CTAs
-                // share an SM
-                int stages = 2;
-                for (int S = 4; S > 2; --S)
-                    if (tma_smem_bytes(tl, S) * 2 <= 228 * 1024) { stages = S; break; }
-                if (to_tma(&tp, 256, 8, stages, false) == SPAGHETTY_OK) *pl = tp;
+        bool done = false;
+        if (allow_tma && spg_box_greedy(fo, 32, 32, 4096, 4096, box) == SPAGHETTY_OK) {
+            int vol = 1;
+            for (int d = 0; d < fo.rank; ++d) vol *= box[d];
+            const int nt = vol <= 1024 ? 128 : 256, ept = vol <= 2048 ? 8 : 16;
+            if (spg_plan(fo, op, box, nt, ept, 0, sms, &tp) == SPAGHETTY_OK &&
+                spg_build_params(&tp, f, g) == SPAGHETTY_OK &&
+                (tp.kind == KIND_TILED || tp.kind == KIND_DIRECT)) {
+                const Plan keep = tp;
+                for (int S = 3; S >= 2 && !done; --S) {
+                    tp = keep;
+                    done = to_tma(&tp, nt, ept, S, false) == SPAGHETTY_OK;
+                }
             }
         }
+        if (!done && spg_box_greedy(fo, 16, 32, 512, 4096, box) == SPAGHETTY_OK) {
+            int vol = 1;
+            for (int d = 0; d < fo.rank; ++d) vol *= box[d];
+            const int nt = vol <= 512 ? 128 : (vol <= 1024 ? 256 : 512), ept = vol <= 2048 ? 4 : 8;
+            done = spg_plan(fo, op, box, nt, ept, 0, sms, &tp) == SPAGHETTY_OK &&
+                   spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_TILED;
+        }
+        if (done) *pl = tp;
     } else if (pl->kind == KIND_DIRECT && allow_tma) {
-        // the stride-1 index stays put: the same-order TMA plan (no
-        // transposition in shared memory) with a box of at most 1K
-        // elements, 128 threads x 8, 2 load stages
         int box[SPG_MAXR];
         Plan tp;
         if (spg_default_box_tma(fo, sms, 1024, box) == SPAGHETTY_OK &&
             spg_plan(fo, op, box, 128, 8, 0, sms, &tp) == SPAGHETTY_OK &&
-            spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_DIRECT &&
-            to_tma(&tp, 128, 8, 2, false) == SPAGHETTY_OK)
-            *pl = tp;
+            spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_DIRECT) {
+            const Plan keep = tp;
+            bool done = false;
+            for (int S = 3; S >= 2 && !done; --S) {
+                tp = keep;
+                done = to_tma(&tp, 128, 8, S, false) == SPAGHETTY_OK;
+            }
+            if (done) *pl = tp;
+        }
     }
     return SPAGHETTY_OK;
 }

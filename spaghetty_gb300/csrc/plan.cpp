@@ -221,7 +221,10 @@ static void choose_box_t(const Shape &s, int64_t nelem, int num_sms, int64_t *L,
         if (d < 0) break;
         int64_t want = std::min<int64_t>(L[d] * 2, L[d] * std::max<int64_t>(2, target / vol));
         int64_t nl = split_len(s.D[d], want);
-        if (vol / L[d] * nl > vmax) nl = largest_divisor_le(s.D[d], vmax * L[d] / vol);
+        if (vol / L[d] * nl > vmax) {
+            if (vtarget > 0) break;      // explicit targets stop at the cap (the autotuner's greedy)
+            nl = largest_divisor_le(s.D[d], vmax * L[d] / vol);
+        }
         if (nl <= L[d]) break;
         L[d] = nl;
     }
@@ -360,6 +363,22 @@ int spg_default_box_tma(const Folded &fo, int num_sms, int vmax, int *box) {
     int64_t vol = 1;
     for (int d = 0; d < R; ++d) vol *= L[d];
     if (vol > vmax) return SPAGHETTY_ERR_CONFIG;
+    for (int d = 0; d < R; ++d) box[d] = (int)L[d];
+    return SPAGHETTY_OK;
+}
+
+// The greedy box with explicit run and volume targets (the autotuner's box
+// family), for the default plans of api.cu.
+int spg_box_greedy(const Folded &fo, int trun_in, int trun_out, int vtarget, int vmax, int *box) {
+    if (fo.empty || fo.rank < 2) return SPAGHETTY_ERR_CONFIG;
+    const int R = fo.rank;
+    Shape s;
+    s.R = R;
+    for (int d = 0; d < R; ++d) { s.D[d] = fo.D[d]; s.in_order[d] = R - 1 - d; }
+    for (int q = 0; q < R; ++q) s.out_order[q] = fo.P[R - 1 - q];
+    int64_t L[SPG_MAXR];
+    choose_box_t(s, fo.nelem, 1, L, vmax, trun_in, trun_out, vtarget);
+    if (volume(s, L) > vmax) return SPAGHETTY_ERR_CONFIG;
     for (int d = 0; d < R; ++d) box[d] = (int)L[d];
     return SPAGHETTY_OK;
 }

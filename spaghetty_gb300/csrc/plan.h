@@ -170,6 +170,7 @@ int spg_plan_batch(const Folded &fo, int op, const SpgBatchRule *rule, Plan *out
 // Installs the tune file beside the library once per process (api.cu).
 void spg_autoload_tune();
 int spg_default_box_tma(const Folded &fo, int num_sms, int vmax, int *box);
+int spg_box_greedy(const Folded &fo, int trun_in, int trun_out, int vtarget, int vmax, int *box);
 int spg_build_params(Plan *pl, double f, double g);
 SpgFactor spg_make_factor(double f, double g);
 int spg_selftest_host(void);

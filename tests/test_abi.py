@@ -86,9 +86,10 @@ def test_plan_invariants_all_rank4_rank6():
         vol = int(np.prod(p["box"]))
         assert vol <= p["threads"] * p["ept"] <= 4096, (dims, perm, p)
         assert all(1 <= b <= d for b, d in zip(p["box"], p["dims"]))
-        # both sides get coalesced rows unless that side is shorter overall
+        # both sides get coalesced rows (at least 16 doubles, 128 bytes)
+        # unless that side is shorter overall
         total = int(np.prod(p["dims"]))
-        assert p["run_in"] >= min(32, total) and p["run_out"] >= min(32, total), (dims, perm, p)
+        assert p["run_in"] >= min(16, total) and p["run_out"] >= min(16, total), (dims, perm, p)
         npartial = sum(1 for b, d in zip(p["box"], p["dims"]) if d % b)
         assert npartial <= 2
         # every plan's shared memory fits one CTA (227 KB opt-in)
