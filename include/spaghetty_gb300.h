@@ -209,6 +209,12 @@ int spaghetty_sort(int rank, const double *unsorted, double *sorted,
 /* Last error recorded by any call on this host thread (0 = none), and a
  * static description of a code. */
 int spaghetty_last_error(void);
+
+/* The CUDA error behind the last SPAGHETTY_ERR_CUDA in this process: a
+ * cudaError_t value, or a negated CUresult when the tensor-map encoding was
+ * rejected; 0 if none.  The string form names it. */
+int spaghetty_last_cuda_error(void);
+const char *spaghetty_last_cuda_error_string(void);
 const char *spaghetty_error_string(int code);
 
 /* Library options.  SPAGHETTY_OPT_HOST_ZERO_COPY (default 1): the

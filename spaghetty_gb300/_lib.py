@@ -85,6 +85,8 @@ PROTOTYPES = {
     "spaghetty_sort": (ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                       c_int_p, c_int_p, ctypes.c_double, ctypes.c_double]),
     "spaghetty_last_error": (ctypes.c_int, []),
+    "spaghetty_last_cuda_error": (ctypes.c_int, []),
+    "spaghetty_last_cuda_error_string": (ctypes.c_char_p, []),
     "spaghetty_device_status": (ctypes.c_int, []),
     "spaghetty_set_option": (ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     "spaghetty_error_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -119,6 +121,9 @@ class SpaghettyError(RuntimeError):
     def __init__(self, code: int, where: str = ""):
         self.code = code
         msg = lib().spaghetty_error_string(code).decode()
+        if code == 7:   # SPAGHETTY_ERR_CUDA: name the CUDA error behind it
+            self.cuda_error = lib().spaghetty_last_cuda_error()
+            msg += " [%s, %d]" % (lib().spaghetty_last_cuda_error_string().decode(), self.cuda_error)
         super().__init__("%s%s (code %d)" % (where + ": " if where else "", msg, code))
 
 

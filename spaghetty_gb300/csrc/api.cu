@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 #include <dlfcn.h>
 
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -43,6 +44,16 @@ const int kMaxSmemPerBlock = 232448;
 int record(int rc) {
     g_last_error = rc;
     return rc;
+}
+
+// The CUDA error behind the last SPAGHETTY_ERR_CUDA (a cudaError_t, or the
+// negated CUresult of a failed tensor-map encoding); process-wide.
+std::atomic<int> g_last_cuda{0};
+
+int cuda_fail(cudaError_t e) {
+    g_last_cuda.store((int)e);
+    cudaGetLastError();
+    return SPAGHETTY_ERR_CUDA;
 }
 
 std::mutex g_mu;
@@ -325,7 +336,11 @@ int encode_map(CUtensorMap *m, const double *ptr, const uint64_t *dim, const uin
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, (void *)ptr, gd, gs, bd, es,
                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS ? SPAGHETTY_OK : SPAGHETTY_ERR_CUDA;
+    if (r != CUDA_SUCCESS) {
+        g_last_cuda.store(-(int)r);
+        return SPAGHETTY_ERR_CUDA;
+    }
+    return SPAGHETTY_OK;
 }
 
 // SPAGHETTY_ERR_DEVICE (and clear) if a kernel reported a timed-out wait.
@@ -369,10 +384,9 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
         if ((rc = encode_map(&mi, u, tl.in_dim, tl.in_stride, tl.in_box))) return rc;
         if ((rc = encode_map(&mo, s, tl.out_dim, tl.out_stride, tl.out_box))) return rc;
         const int smem = tma_smem_bytes(tl, pl.stages);
-        if (smem > 48 * 1024 &&
-            cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) {
-            cudaGetLastError();
-            return SPAGHETTY_ERR_CUDA;
+        if (smem > 48 * 1024) {
+            const cudaError_t e = cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+            if (e != cudaSuccess) return cuda_fail(e);
         }
         const int occ = occupancy(k, smem);
         int64_t grid = std::min<int64_t>((int64_t)pl.kp.ntiles, (int64_t)sms * occ);
@@ -384,11 +398,9 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
         const SpgKernelEntry *k = find_kernel(pl.kind, pl.op, pl.threads, pl.ept, pl.stages);
         if (!k) return SPAGHETTY_ERR_NOKERNEL;
         if (pl.smem_bytes > 48 * 1024) {
-            if (cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     pl.smem_bytes) != cudaSuccess) {
-                cudaGetLastError();
-                return SPAGHETTY_ERR_CUDA;
-            }
+            const cudaError_t e =
+                cudaFuncSetAttribute(k->fn, cudaFuncAttributeMaxDynamicSharedMemorySize, pl.smem_bytes);
+            if (e != cudaSuccess) return cuda_fail(e);
         }
         const int occ = occupancy(k, pl.smem_bytes);
         int64_t grid = std::min<int64_t>((int64_t)pl.kp.ntiles, (int64_t)sms * occ);
@@ -398,10 +410,7 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
         err = cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(pl.threads), args,
                                (size_t)pl.smem_bytes, st);
     }
-    if (err != cudaSuccess) {
-        cudaGetLastError();
-        return SPAGHETTY_ERR_CUDA;
-    }
+    if (err != cudaSuccess) return cuda_fail(err);
     return SPAGHETTY_OK;
 }
 
@@ -763,6 +772,14 @@ const char *spaghetty_error_string(int code) {
 }
 
 int spaghetty_last_error(void) { return g_last_error; }
+
+int spaghetty_last_cuda_error(void) { return g_last_cuda.load(); }
+
+const char *spaghetty_last_cuda_error_string(void) {
+    const int e = g_last_cuda.load();
+    if (e < 0) return "tensor-map encoding rejected its arguments";
+    return cudaGetErrorString((cudaError_t)e);
+}
 
 int spaghetty_set_option(int option, int value) {
     if (option == SPAGHETTY_OPT_HOST_ZERO_COPY) {
