@@ -194,8 +194,10 @@ int tce_sortacc_6_status(const double *unsorted, double *sorted,
  *     acc_factor == 1:  sorted = sorted + factor*unsorted
  *     otherwise:        sorted = acc_factor*sorted + factor*unsorted
  * `dims` and `perm` are host arrays of `rank` ints (perm 1-based).
- * Both tensor pointers must be device pointers; the work is enqueued on
- * `stream` (a cudaStream_t, NULL = legacy default stream) and the call
+ * Both tensor pointers must be device (or managed) memory of one device,
+ * else SPAGHETTY_ERR_MEMSPACE; the work runs on that device whatever the
+ * calling thread's current device is, and is enqueued on `stream` (a
+ * cudaStream_t of that device, NULL = legacy default stream); the call
  * returns without waiting.  Returns a SPAGHETTY_* code. */
 int spaghetty_sort_async(int rank, const double *unsorted, double *sorted,
                          const int *dims, const int *perm,
@@ -307,7 +309,8 @@ int spaghetty_selftest(void);
  * sortaccs per t3 tile (branches/spaghetty2/ccsd_t_tce_sort_list.txt).
  * dims: nsrc*rank source dims, as each tce_sortacc call would pass them;
  * perms: nsrc*rank, 1-based; every permuted shape must equal the output's.
- * rank <= 6, nsrc <= 16.  Device pointers; asynchronous on `stream`. */
+ * rank <= 6, nsrc <= 16.  Device (or managed) memory of one device, else
+ * SPAGHETTY_ERR_MEMSPACE; runs on that device, asynchronous on `stream`. */
 int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *unsorted,
                             const int *dims, const int *perms, const double *factors,
                             double *sorted, void *stream);

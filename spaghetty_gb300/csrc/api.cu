@@ -743,6 +743,22 @@ void autoload_tune_file() {
 // it before planning a batch, so that its size-bucket rules apply).
 void spg_autoload_tune() { autoload_tune_file(); }
 
+// The asynchronous sort for pointers already known to be device memory of
+// device `dev`, the current device of the calling thread (the batched
+// plain path, which validated them when the batch was created).
+int spg_sort_async_on(int dev, int rank, const double *unsorted, double *sorted, const int *dims,
+                      const int *perm, double factor, double acc_factor, void *stream) {
+    Folded fo;
+    int rc = spg_fold(rank, dims, perm, &fo);
+    if (rc) return rc;
+    if (fo.empty) return SPAGHETTY_OK;
+    Plan pl;
+    rc = make_plan(rank, dims, perm, factor, acc_factor, device_sms(dev), &pl,
+                   aligned16(unsorted) && aligned16(sorted));
+    if (rc) return rc;
+    return launch_plan(pl, unsorted, sorted, (cudaStream_t)stream, dev);
+}
+
 // ===========================================================================
 extern "C" {
 
@@ -813,13 +829,24 @@ int spaghetty_sort_async(int rank, const double *unsorted, double *sorted, const
     if (fo.empty) return record(SPAGHETTY_OK);
     if (!unsorted || !sorted) return record(SPAGHETTY_ERR_NULL);
     if (overlaps(unsorted, sorted, fo.nelem)) return record(SPAGHETTY_ERR_ALIAS);
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return record(SPAGHETTY_ERR_CUDA); }
+    // the asynchronous form works on device (or managed) memory of one
+    // device, and runs on that device whatever the calling thread's current
+    // device is: setting it also binds its context to a thread that has
+    // none yet (a worker thread of the caller), which the tensor-map
+    // encoding needs
+    int du = -1, ds = -1;
+    if (classify(unsorted, &du, nullptr) != 1 || classify(sorted, &ds, nullptr) != 1 || du != ds)
+        return record(SPAGHETTY_ERR_MEMSPACE);
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) cudaGetLastError();
+    cudaError_t e = cudaSetDevice(du);
+    if (e != cudaSuccess) return record(cuda_fail(e));
     Plan pl;
-    rc = make_plan(rank, dims, perm, factor, acc_factor, device_sms(dev), &pl,
+    rc = make_plan(rank, dims, perm, factor, acc_factor, device_sms(du), &pl,
                    aligned16(unsorted) && aligned16(sorted));
-    if (rc) return record(rc);
-    return record(launch_plan(pl, unsorted, sorted, (cudaStream_t)stream, dev));
+    if (!rc) rc = launch_plan(pl, unsorted, sorted, (cudaStream_t)stream, du);
+    if (cur >= 0 && cur != du) cudaSetDevice(cur);
+    return record(rc);
 }
 
 int spaghetty_sort(int rank, const double *unsorted, double *sorted, const int *dims,

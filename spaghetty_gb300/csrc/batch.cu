@@ -419,12 +419,20 @@ int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
 
 int spaghetty_batch_launch_plain(spaghetty_batch *b, void *stream) {
     if (!b) return SPAGHETTY_ERR_NULL;
-    for (const spaghetty_batch_entry &e : b->entries) {
-        int rc = spaghetty_sort_async(e.rank, e.unsorted, e.sorted, e.dims, e.perm, e.factor,
-                                      e.acc_factor, stream);
-        if (rc) return rc;
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) cudaGetLastError();
+    if (cudaSetDevice(b->dev) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
     }
-    return SPAGHETTY_OK;
+    int rc = SPAGHETTY_OK;
+    for (const spaghetty_batch_entry &e : b->entries) {
+        rc = spg_sort_async_on(b->dev, e.rank, e.unsorted, e.sorted, e.dims, e.perm, e.factor,
+                               e.acc_factor, stream);
+        if (rc) break;
+    }
+    if (cur >= 0 && cur != b->dev) cudaSetDevice(cur);
+    return rc;
 }
 
 int spaghetty_batch_status(spaghetty_batch *b, void *stream) {

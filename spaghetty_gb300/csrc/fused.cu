@@ -443,14 +443,42 @@ extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *
                 if (perms[k * rank + q] == i + 1) fast[k] = q;
         }
     }
+    {
+        int64_t n0 = 1;
+        for (int q = 0; q < rank; ++q) n0 *= dims[q] > 0 ? dims[q] : 0;
+        if (n0 == 0) return SPAGHETTY_OK;   // empty tensors: nothing to do
+    }
+    // device (or managed) memory of one device only: the kernel reads and
+    // writes these pointers directly; the work runs on that device
+    int dev = -1;
+    for (int k = -1; k < nsrc; ++k) {
+        const void *ptr = k < 0 ? (const void *)sorted : (const void *)unsorted[k];
+        if (!ptr) return SPAGHETTY_ERR_NULL;
+        cudaPointerAttributes at;
+        std::memset(&at, 0, sizeof(at));
+        if (cudaPointerGetAttributes(&at, ptr) != cudaSuccess) {
+            cudaGetLastError();
+            return SPAGHETTY_ERR_MEMSPACE;
+        }
+        if ((at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) || (dev >= 0 && at.device != dev))
+            return SPAGHETTY_ERR_MEMSPACE;
+        dev = at.device;
+    }
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) cudaGetLastError();
+    if (cudaSetDevice(dev) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    int rc = SPAGHETTY_OK;
     int k0 = 0;
-    while (k0 < nsrc) {
+    while (k0 < nsrc && rc == SPAGHETTY_OK) {
         int k1 = k0 + 1;
         while (k1 < nsrc && fast[k1] == fast[k0]) ++k1;
-        const int rc = fused_pass(rank, k1 - k0, unsorted + k0, dims + k0 * rank, perms + k0 * rank,
-                                  factors + k0, sorted, stream);
-        if (rc) return rc;
+        rc = fused_pass(rank, k1 - k0, unsorted + k0, dims + k0 * rank, perms + k0 * rank,
+                        factors + k0, sorted, stream);
         k0 = k1;
     }
-    return SPAGHETTY_OK;
+    if (cur >= 0 && cur != dev) cudaSetDevice(cur);
+    return rc;
 }

@@ -169,6 +169,9 @@ struct SpgBatchRule {
 int spg_plan_batch(const Folded &fo, int op, const SpgBatchRule *rule, Plan *out);
 // Installs the tune file beside the library once per process (api.cu).
 void spg_autoload_tune();
+// Asynchronous sort of device pointers of device `dev` (api.cu), no pointer checks.
+int spg_sort_async_on(int dev, int rank, const double *unsorted, double *sorted, const int *dims,
+                      const int *perm, double factor, double acc_factor, void *stream);
 int spg_default_box_tma(const Folded &fo, int num_sms, int vmax, int *box);
 int spg_box_greedy(const Folded &fo, int trun_in, int trun_out, int vtarget, int vmax, int *box);
 int spg_build_params(Plan *pl, double f, double g);

@@ -70,6 +70,24 @@ def test_backward_bit_exact_and_finite_differences(cuda, dims):
     assert worst < 1e-8, worst
 
 
+def test_backward_on_autograd_thread_bench_perms(cuda):
+    """The benchmark's perms at 24^4 (4321 runs on the TMA-staged kernel);
+    the backward runs on the autograd engine's own worker thread."""
+    from spaghetty_gb300.autograd import permute_sum, reference_grad
+    dims = (24, 24, 24, 24)
+    perms = [(4, 3, 2, 1), (2, 4, 1, 3), (3, 1, 4, 2)]
+    factors = (0.75, -1.25, 0.3)
+    g = torch.Generator().manual_seed(3)
+    xh = torch.rand(dims, dtype=torch.float64, generator=g) - 0.5
+    dyh = torch.rand(dims, dtype=torch.float64, generator=g)
+    x = xh.to(cuda).requires_grad_(True)
+    for _ in range(2):
+        x.grad = None
+        y = permute_sum(x, perms, factors)
+        y.backward(dyh.to(cuda))
+    assert torch.equal(x.grad.detach().cpu(), reference_grad(dyh, perms, factors))
+
+
 def test_single_permute_gradcheck(cuda):
     from spaghetty_gb300.autograd import permute
     x = torch.rand((3, 4, 5, 2), dtype=torch.float64, device=cuda, requires_grad=True)

@@ -372,3 +372,34 @@ def test_every_forced_variant_rank4(cuda, dims):
         clear()
     assert ran["tma"] > 0 and ran["other"] > 0
     assert lib().spaghetty_device_status() == 0
+
+
+def test_async_form_checks_memory_and_binds_device(cuda):
+    """The asynchronous entry refuses host memory (no launch on a pointer
+    the GPU cannot read) and works from a fresh host thread that has no
+    CUDA context yet (the tensor-map encoding needs one)."""
+    import threading
+    L = lib()
+    dims = (24, 24, 24, 24)
+    n = int(np.prod(dims))
+    uh = O.seeded_uniform(n, 41)
+    sh = np.zeros(n)
+    rc = L.spaghetty_sort_async(4, uh.ctypes.data_as(ctypes.c_void_p), sh.ctypes.data_as(ctypes.c_void_p),
+                                int_array(dims), int_array((4, 3, 2, 1)), 0.5, 0.0, None)
+    assert rc == 8 and not sh.any()      # SPAGHETTY_ERR_MEMSPACE
+    du = dev(uh, cuda)
+    want = O.np_sort(uh, dims, (4, 3, 2, 1), 0.75, 0.0)
+    out = {}
+
+    s = torch.empty(n, dtype=torch.float64, device=cuda)
+    torch.cuda.synchronize()
+
+    def worker():   # only the library touches CUDA on this thread
+        out["rc"] = L.spaghetty_sort_async(4, ctypes.c_void_p(du.data_ptr()), ctypes.c_void_p(s.data_ptr()),
+                                           int_array(dims), int_array((4, 3, 2, 1)), 0.75, 0.0, None)
+
+    t = threading.Thread(target=worker)
+    t.start()
+    t.join()
+    assert out["rc"] == 0, L.spaghetty_last_cuda_error()
+    check(host(s), want, "async sort from a fresh thread")
