@@ -721,8 +721,21 @@ def run_fused_case(args):
                       "gbs": round((16 * n + 72 * n) / t / 1e9, 1)}), flush=True)
 
 
+def run_batched_case(args):
+    """A reduced batched mix (profiling workload): --batched-case
+    N:E4LO-E4HI:E6LO-E6HI, e.g. 512:8-40:6-12."""
+    import torch
+    n_s, e4, e6 = args.batched_case.split(":")
+    ext4 = tuple(int(x) for x in e4.split("-"))
+    ext6 = tuple(int(x) for x in e6.split("-"))
+    r = run_batched(args, torch.device("cuda", 0), ext4=ext4, ext6=ext6, n=int(n_s))
+    print(json.dumps({"batched_case": args.batched_case, **r}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--batched-case", default=None,
+                    help="N:E4LO-E4HI:E6LO-E6HI: time one reduced batched mix")
     ap.add_argument("--fused-case", default=None, help="GROUP:EXTENT: time one fused triples group")
     ap.add_argument("--case", default=None,
                     help="dims:perm:op[:factor] (op 0 sort, 1 sortacc; factor 0.5): time one case")
@@ -743,6 +756,9 @@ def main():
         return
     if args.fused_case:
         run_fused_case(args)
+        return
+    if args.batched_case:
+        run_batched_case(args)
         return
     if args.impl == "reference":
         line = run_reference(args, ws, rank)
