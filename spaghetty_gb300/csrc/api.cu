@@ -236,11 +236,14 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
     //    box with 16/32-double rows towards 512 elements;
     //  - the stride-1 index unchanged: the same-order TMA plan on a box of
     //    at most 1K elements, 128 threads x 8, 3 load stages (else 2).
-    if (pl->kind == KIND_TILED) {
+    // Host-mapped (zero-copy) and misaligned buffers cannot use the bulk
+    // copies: they keep the planner's own plan (the cp.async pipeline with
+    // its larger boxes keeps the most bytes in flight over the host link).
+    if (pl->kind == KIND_TILED && allow_tma) {
         int box[SPG_MAXR];
         Plan tp;
         bool done = false;
-        if (allow_tma && spg_box_greedy(fo, 32, 32, 4096, 4096, box) == SPAGHETTY_OK) {
+        if (spg_box_greedy(fo, 32, 32, 4096, 4096, box) == SPAGHETTY_OK) {
             int vol = 1;
             for (int d = 0; d < fo.rank; ++d) vol *= box[d];
             const int nt = vol <= 1024 ? 128 : 256, ept = vol <= 2048 ? 8 : 16;
@@ -255,6 +258,7 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
             }
         }
         if (!done && spg_box_greedy(fo, 16, 32, 512, 4096, box) == SPAGHETTY_OK) {
+            // no TMA plan fits (strides or box rows not multiples of 16 bytes)
             int vol = 1;
             for (int d = 0; d < fo.rank; ++d) vol *= box[d];
             const int nt = vol <= 512 ? 128 : (vol <= 1024 ? 256 : 512), ept = vol <= 2048 ? 4 : 8;
