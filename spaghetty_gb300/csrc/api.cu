@@ -330,7 +330,7 @@ int *status_word_dev() {
 }
 
 int encode_map(CUtensorMap *m, const double *ptr, const uint64_t *dim, const uint64_t *stride,
-               const uint32_t *box) {
+               const uint32_t *box, bool swizzle128 = false) {
     EncodeTiledFn fn = encode_fn();
     if (!fn) return SPAGHETTY_ERR_CUDA;
     cuuint64_t gd[5], gs[4];
@@ -338,7 +338,8 @@ int encode_map(CUtensorMap *m, const double *ptr, const uint64_t *dim, const uin
     for (int k = 0; k < 5; ++k) { gd[k] = dim[k]; bd[k] = box[k]; es[k] = 1; }
     for (int k = 0; k < 4; ++k) gs[k] = stride[k + 1];
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, (void *)ptr, gd, gs, bd, es,
-                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                     CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         g_last_cuda.store(-(int)r);
@@ -746,6 +747,13 @@ void autoload_tune_file() {
 // Installs the tune file beside the library once per process (batch.cu calls
 // it before planning a batch, so that its size-bucket rules apply).
 void spg_autoload_tune() { autoload_tune_file(); }
+
+// Tensor-map encoding and the kernels' status word, for fused.cu.
+int spg_encode_map(CUtensorMap *m, const double *ptr, const uint64_t *dim, const uint64_t *stride,
+                   const uint32_t *box, int swizzle128) {
+    return encode_map(m, ptr, dim, stride, box, swizzle128 != 0);
+}
+int *spg_status_word() { return status_word_dev(); }
 
 // The asynchronous sort for pointers already known to be device memory of
 // device `dev`, the current device of the calling thread (the batched

@@ -23,6 +23,7 @@
 #include "../../include/spaghetty_gb300.h"
 #include "kernels.cuh"
 #include "plan.h"
+#include "tma.cuh"
 
 #include <cuda_runtime.h>
 
@@ -178,6 +179,201 @@ spg_fused_sortacc(double *__restrict__ out, const __grid_constant__ FusedParams 
 }
 
 // ===========================================================================
+// TMA-staged form of one pass.  The box spans two output dims: the one the
+// pass's sources hold stride-1 (p, 16 elements) and the output's stride-1
+// dim (q, lq elements); every other dim has box length 1.  Every source
+// tile then has the same layout, [p fastest (16 doubles = one 128-byte
+// row), q], so one index per element serves every source; the tiles are
+// loaded with the 128-byte swizzle, which spreads the q-strided reads of a
+// warp over the banks.  The old output tile and the result are in output
+// order, [q fastest, p].
+//
+// Warp-specialised like spg_tiled_tma: a load thread streams the items of
+// each box (old output tile, then source 0..nsrc-1) through a ring of S
+// slots ("full" / "empty" mbarriers); NT permute threads add the items in
+// order into registers and write the result to one of two output slots
+// ("done" / "free"); a store thread stores it.  Every wait is bounded.
+#define SPG_FT_MAXS 16
+#define SPG_FT_BLOCK(NT) ((NT) + 64)
+
+struct FusedTmaParams {
+    uint32_t ntiles;
+    int32_t ng;                                    // grid dims, fastest first
+    FastDiv gcnt[SPG_FUSED_MAXR];
+    int8_t mdim[SPG_FT_MAXS + 1][SPG_FUSED_MAXR];  // per map (0 = output) and grid dim
+    int32_t mul[SPG_FT_MAXS + 1][SPG_FUSED_MAXR];  // map coordinate step per box
+    int32_t nsrc, vol, lq;
+    uint32_t tile_bytes;                           // one slot, 1024-aligned
+    uint32_t tx;                                   // bytes one load delivers
+    SpgFactor fac[SPG_FT_MAXS];
+    int32_t op[SPG_FT_MAXS];
+    int *status;
+};
+
+struct FusedTmaMaps {
+    CUtensorMap m[SPG_FT_MAXS + 1];                // 0 = output, 1.. = sources
+};
+
+__device__ __forceinline__ void spg_ft_coords(const FusedTmaParams &p, int map, uint32_t t, int32_t *c) {
+#pragma unroll
+    for (int m = 0; m < 5; ++m) c[m] = 0;
+#pragma unroll
+    for (int k = 0; k < SPG_FUSED_MAXR; ++k) {
+        if (k < p.ng) {
+            const uint32_t q = fd_div(t, p.gcnt[k]);
+            const uint32_t x = t - q * p.gcnt[k].d;
+            t = q;
+#pragma unroll
+            for (int m = 0; m < 5; ++m)
+                if (p.mdim[map][k] == m) c[m] += (int32_t)x * p.mul[map][k];
+        }
+    }
+}
+
+template <int NT, int EPT, int S>
+__global__ void __launch_bounds__(SPG_FT_BLOCK(NT))
+spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__ FusedTmaParams p) {
+    extern __shared__ __align__(1024) unsigned char smem_raw0[];
+    const uint32_t raw = (uint32_t)__cvta_generic_to_shared(smem_raw0);
+    const uint32_t base = (raw + 1023u) & ~1023u;
+    unsigned char *smem = smem_raw0 + (base - raw);
+    const uint32_t tb = p.tile_bytes;
+    const uint32_t out0 = (uint32_t)S * tb;
+    const uint32_t full0 = base + out0 + 2u * tb;
+    const uint32_t empty0 = full0 + 8u * S;
+    const uint32_t done0 = empty0 + 8u * S;
+    const uint32_t free0 = done0 + 16u;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t G = gridDim.x;
+    const int items = p.nsrc + 1;
+    const uint32_t load_tid = NT, store_tid = NT + 32;
+
+    if (tid == load_tid) {
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+            spg_mbar_init(full0 + 8u * s, 1u);
+            spg_mbar_init(empty0 + 8u * s, (uint32_t)(NT / 32));
+        }
+#pragma unroll
+        for (int o = 0; o < 2; ++o) {
+            spg_mbar_init(done0 + 8u * o, (uint32_t)(NT / 32));
+            spg_mbar_init(free0 + 8u * o, 1u);
+        }
+        spg_fence_mbar_init();
+    }
+    // permute threads: output-order element e = tid + m*NT of the box is
+    // (xq, xp) = (e % lq, e / lq); its byte offset in a (swizzled) source
+    // tile is ((xp + 16*xq) * 8) with the 16-byte chunk index XOR row % 8
+    uint32_t soff[EPT];
+#pragma unroll
+    for (int m = 0; m < EPT; ++m) {
+        const uint32_t e = tid + (uint32_t)m * NT;
+        soff[m] = 0xFFFFFFFFu;
+        if (tid < NT && e < (uint32_t)p.vol) {
+            const uint32_t xq = e % (uint32_t)p.lq, xp = e / (uint32_t)p.lq;
+            const uint32_t o = (xp + 16u * xq) * 8u;
+            soff[m] = o ^ ((xq & 7u) << 4);
+        }
+    }
+    __syncthreads();                        // barriers initialised before anyone waits
+
+    if (tid == load_tid) {
+        // ---- loads: item i of box it goes to slot j % S, j = it*items + i ----
+        bool ok = true;
+        int64_t j = 0;
+        int it = 0;
+        for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += G, ++it) {
+            for (int i = 0; i < items; ++i, ++j) {
+                const int s = (int)(j % S);
+                if (j >= S) {
+                    ok = spg_mbar_wait(empty0 + 8u * (uint32_t)s, (uint32_t)(((j / S) - 1) & 1));
+                    if (!ok) break;
+                }
+                int32_t c[5];
+                spg_ft_coords(p, i, t, c);
+                const uint32_t mb = full0 + 8u * (uint32_t)s;
+                spg_mbar_expect_tx(mb, p.tx);
+                spg_tma_load5(base + (uint32_t)s * tb, &maps.m[i], c, mb);
+            }
+        }
+        if (!ok && p.status) *(volatile int *)p.status = 1;
+        // the CTA must not retire with a load in flight
+        for (int64_t q = j > S ? j - S : 0; q < j; ++q)
+            spg_mbar_wait(full0 + 8u * (uint32_t)(q % S), (uint32_t)((q / S) & 1));
+        return;
+    }
+    if (tid == store_tid) {
+        bool ok = true;
+        int it = 0;
+        for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
+            const int o = it & 1;
+            ok = spg_mbar_wait(done0 + 8u * (uint32_t)o, (uint32_t)((it >> 1) & 1));
+            if (!ok) break;
+            int32_t c[5];
+            spg_ft_coords(p, 0, t, c);
+            spg_tma_store5(&maps.m[0], c, base + out0 + (uint32_t)o * tb);
+            spg_bulk_commit();
+            spg_bulk_wait_read<0>();
+            spg_mbar_arrive(free0 + 8u * (uint32_t)o);
+        }
+        if (!ok && p.status) *(volatile int *)p.status = 1;
+        spg_bulk_wait0();
+        return;
+    }
+    if (tid >= NT) return;
+
+    // ---- permute threads ----
+    const uint32_t lane = tid & 31u;
+    int64_t j = 0;
+    int it = 0;
+    bool ok = true;
+    for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += G, ++it) {
+        double acc[EPT];
+        for (int i = 0; i < items; ++i, ++j) {
+            const int s = (int)(j % S);
+            ok = __all_sync(0xffffffffu, spg_mbar_wait(full0 + 8u * (uint32_t)s, (uint32_t)((j / S) & 1)));
+            if (!ok) break;
+            const unsigned char *slot = smem + (size_t)s * tb;
+            if (i == 0) {
+                const double *told = reinterpret_cast<const double *>(slot);
+#pragma unroll
+                for (int m = 0; m < EPT; ++m) {
+                    const uint32_t e = tid + (uint32_t)m * NT;
+                    acc[m] = soff[m] != 0xFFFFFFFFu ? told[e] : 0.0;
+                }
+            } else {
+                const SpgFactor F = p.fac[i - 1];
+                const int op = p.op[i - 1];
+#pragma unroll
+                for (int m = 0; m < EPT; ++m)
+                    if (soff[m] != 0xFFFFFFFFu)
+                        acc[m] = spg_fused_apply(op, acc[m], *reinterpret_cast<const double *>(slot + soff[m]), F);
+            }
+            __syncwarp();
+            if (lane == 0) spg_mbar_arrive(empty0 + 8u * (uint32_t)s);
+        }
+        if (!ok) break;
+        const int o = it & 1;
+        ok = __all_sync(0xffffffffu, spg_mbar_wait(free0 + 8u * (uint32_t)o, (uint32_t)(((it >> 1) & 1) ^ 1)));
+        if (!ok) break;
+        double *tout = reinterpret_cast<double *>(smem + out0 + (size_t)o * tb);
+#pragma unroll
+        for (int m = 0; m < EPT; ++m) {
+            const uint32_t e = tid + (uint32_t)m * NT;
+            if (soff[m] != 0xFFFFFFFFu) tout[e] = acc[m];
+        }
+        spg_fence_async_smem();
+        __syncwarp();
+        if (lane == 0) spg_mbar_arrive(done0 + 8u * (uint32_t)o);
+    }
+    if (!ok && p.status) *(volatile int *)p.status = 1;
+}
+
+#define SPG_FT_NT 256
+#define SPG_FT_EPT 4
+#define SPG_FT_S 8
+
+// ===========================================================================
 namespace {
 
 // Grow box lengths over the output dims (divisors of the extents) until the
@@ -244,6 +440,153 @@ void fused_box(int R, const int64_t *O, int nl, const int (*order)[SPG_FUSED_MAX
 
 }  // namespace
 
+// One tensor map for the TMA-staged pass: dims in memory order (fastest
+// first: index into the kept output dims), their extents, element strides
+// and box lengths.  Consecutive dims merge into one map dim when they
+// continue its memory range and the map dim so far is covered in full or
+// has box length 1 (never into map dim 0 when `lone_inner`, which the
+// swizzled source tiles need).  Fills per-kept-dim map dim and coordinate
+// weight; returns false when the bulk copy's rules are not met.
+static bool ft_map(int R, const int *order, const int64_t *ext, const int64_t *str, const int64_t *L,
+                   bool lone_inner, uint64_t *dim, uint64_t *stride, uint32_t *box, int8_t *mdim,
+                   int64_t *weight) {
+    int m = -1;
+    bool full = false, unit = false;
+    for (int q = 0; q < R; ++q) {
+        const int d = order[q];
+        bool merge = m >= 0 && !(lone_inner && m == 0) && (uint64_t)str[d] * 8u == stride[m] * dim[m] &&
+                     (full || (unit && L[d] == 1));
+        if (merge) {
+            weight[d] = (int64_t)dim[m];
+            dim[m] *= (uint64_t)ext[d];
+            box[m] = (uint32_t)((int64_t)box[m] * L[d]);
+            full = full && L[d] == ext[d];
+            unit = unit && L[d] == 1;
+        } else {
+            if (++m >= 5) return false;
+            dim[m] = (uint64_t)ext[d];
+            box[m] = (uint32_t)L[d];
+            stride[m] = (uint64_t)str[d] * 8u;
+            weight[d] = 1;
+            full = L[d] == ext[d];
+            unit = L[d] == 1;
+        }
+        mdim[d] = (int8_t)m;
+    }
+    const int n = m + 1;
+    for (int k = 0; k < n; ++k) {
+        if (box[k] < 1 || box[k] > 256 || dim[k] > ((uint64_t)1 << 31)) return false;
+        if (k > 0 && (stride[k] % 16 != 0 || stride[k] >= ((uint64_t)1 << 40))) return false;
+    }
+    if (stride[0] != 8 || (box[0] * 8u) % 16u != 0) return false;
+    for (int k = n; k < 5; ++k) {
+        dim[k] = 1;
+        box[k] = 1;
+        stride[k] = stride[k - 1] * dim[k - 1];
+        if (stride[k] >= ((uint64_t)1 << 40)) return false;
+    }
+    return true;
+}
+
+// The TMA-staged pass, or SPAGHETTY_ERR_NOKERNEL when the shapes or the
+// buffers do not allow it (the caller then runs the cp.async kernel).
+// O, ostr: kept output dims (output order) and their element strides;
+// sstr[k]: each kept dim's element stride in source k.
+static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
+                          int nsrc, const double *const *unsorted, const double *factors, double *sorted,
+                          void *stream) {
+    if (R < 2 || nsrc < 1 || nsrc > SPG_FT_MAXS) return SPAGHETTY_ERR_NOKERNEL;
+    if (((uintptr_t)sorted & 15u) != 0) return SPAGHETTY_ERR_NOKERNEL;
+    for (int k = 0; k < nsrc; ++k)
+        if (((uintptr_t)unsorted[k] & 15u) != 0) return SPAGHETTY_ERR_NOKERNEL;
+    const int q = R - 1;                    // output stride-1 dim
+    int p = -1;                             // the sources' stride-1 dim
+    for (int i = 0; i < R && p < 0; ++i) {
+        bool all = true;
+        for (int k = 0; k < nsrc; ++k) all = all && sstr[k][i] == 1;
+        if (all) p = i;
+    }
+    if (p < 0 || p == q || O[p] < 16 || O[q] < 8) return SPAGHETTY_ERR_NOKERNEL;
+    int64_t lq = std::min<int64_t>(O[q], 64);
+    lq &= ~(int64_t)1;
+    int64_t L[SPG_FUSED_MAXR];
+    for (int i = 0; i < R; ++i) L[i] = 1;
+    L[p] = 16;
+    L[q] = lq;
+    const int64_t vol = 16 * lq;
+    if (vol > SPG_FT_NT * SPG_FT_EPT) return SPAGHETTY_ERR_NOKERNEL;
+    static thread_local FusedTmaParams P;
+    static thread_local FusedTmaMaps M;
+    std::memset(&P, 0, sizeof(P));
+    // grid: kept dims with more than one box, output order fastest first
+    int gd[SPG_FUSED_MAXR];
+    int ng = 0;
+    int64_t ntiles = 1;
+    for (int i = R - 1; i >= 0; --i) {
+        const int64_t c = (O[i] + L[i] - 1) / L[i];
+        if (c <= 1) continue;
+        gd[ng] = i;
+        P.gcnt[ng] = spg_make_fastdiv((uint32_t)c);
+        ++ng;
+        ntiles *= c;
+        if (ntiles > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
+    }
+    P.ng = ng;
+    P.ntiles = (uint32_t)ntiles;
+    // maps: 0 = output (output order), 1.. = sources (their memory order)
+    for (int mi = 0; mi <= nsrc; ++mi) {
+        int order[SPG_FUSED_MAXR];
+        const int64_t *str = mi == 0 ? ostr : sstr[mi - 1];
+        for (int i = 0; i < R; ++i) order[i] = i;
+        std::sort(order, order + R, [&](int a, int b) { return str[a] < str[b]; });
+        uint64_t dim[5], stride[5];
+        uint32_t box[5];
+        int8_t mdim[SPG_FUSED_MAXR];
+        int64_t w[SPG_FUSED_MAXR];
+        if (!ft_map(R, order, O, str, L, mi > 0, dim, stride, box, mdim, w)) return SPAGHETTY_ERR_NOKERNEL;
+        if (mi > 0 && box[0] != 16) return SPAGHETTY_ERR_NOKERNEL;   // one 128-byte swizzled row
+        for (int g = 0; g < ng; ++g) {
+            const int i = gd[g];
+            const int64_t mul = L[i] * w[i];
+            if (mul * ((O[i] + L[i] - 1) / L[i]) > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
+            P.mdim[mi][g] = mdim[i];
+            P.mul[mi][g] = (int32_t)mul;
+        }
+        const double *ptr = mi == 0 ? sorted : unsorted[mi - 1];
+        if (spg_encode_map(&M.m[mi], ptr, dim, stride, box, mi > 0) != SPAGHETTY_OK) return SPAGHETTY_ERR_NOKERNEL;
+    }
+    P.nsrc = nsrc;
+    P.vol = (int32_t)vol;
+    P.lq = (int32_t)lq;
+    P.tile_bytes = (uint32_t)(((vol * 8) + 1023) & ~(int64_t)1023);
+    P.tx = (uint32_t)(vol * 8);
+    for (int k = 0; k < nsrc; ++k) {
+        P.fac[k] = spg_make_factor(factors[k], 1.0);
+        P.op[k] = spg_choose_op(factors[k], 1.0);
+    }
+    P.status = spg_status_word();
+    const size_t smem = (size_t)(SPG_FT_S + 2) * P.tile_bytes + (2 * SPG_FT_S + 4) * 8 + 1024;
+    const void *fn = (const void *)spg_fused_tma<SPG_FT_NT, SPG_FT_EPT, SPG_FT_S>;
+    if (smem > 48 * 1024 && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    int dev = 0, sms = 152, nb = 1;
+    if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 152;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, SPG_FT_BLOCK(SPG_FT_NT), smem) != cudaSuccess || nb < 1)
+        nb = 1;
+    cudaGetLastError();
+    const int grid = (int)std::min<int64_t>((int64_t)sms * nb, ntiles);
+    void *args[] = {(void *)&M, (void *)&P};
+    if (cudaLaunchKernel(fn, dim3(grid), dim3(SPG_FT_BLOCK(SPG_FT_NT)), args, smem, (cudaStream_t)stream) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return SPAGHETTY_ERR_CUDA;
+    }
+    return SPAGHETTY_OK;
+}
+
 static int fused_pass(int rank, int nsrc, const double *const *unsorted, const int *dims,
                       const int *perms, const double *factors, double *sorted, void *stream) {
     if (rank < 1 || rank > SPG_FUSED_MAXR) return SPAGHETTY_ERR_RANK;
@@ -296,6 +639,10 @@ static int fused_pass(int rank, int nsrc, const double *const *unsorted, const i
     }
     int64_t ostr[SPG_FUSED_MAXR];
     for (int i = 0; i < R; ++i) ostr[i] = ostride_full[keep[i]];
+    {
+        const int rc = fused_tma_pass(R, O, ostr, sstride, nsrc, unsorted, factors, sorted, stream);
+        if (rc != SPAGHETTY_ERR_NOKERNEL) return rc;
+    }
     // layouts: 0 = output, 1.. = sources; each lists the kept dims fastest first
     int order[SPG_FUSED_MAXS + 1][SPG_FUSED_MAXR];
     for (int i = 0; i < R; ++i) order[0][i] = R - 1 - i;

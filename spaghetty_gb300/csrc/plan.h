@@ -169,6 +169,12 @@ struct SpgBatchRule {
 int spg_plan_batch(const Folded &fo, int op, const SpgBatchRule *rule, Plan *out);
 // Installs the tune file beside the library once per process (api.cu).
 void spg_autoload_tune();
+// Tensor-map encoding (5 dims, FP64; swizzle128: 128-byte swizzle) and the
+// device address of the kernels' status word (api.cu).
+struct CUtensorMap_st;
+int spg_encode_map(CUtensorMap_st *m, const double *ptr, const uint64_t *dim, const uint64_t *stride,
+                   const uint32_t *box, int swizzle128);
+int *spg_status_word();
 // Asynchronous sort of device pointers of device `dev` (api.cu), no pointer checks.
 int spg_sort_async_on(int dev, int rank, const double *unsorted, double *sorted, const int *dims,
                       const int *perm, double factor, double acc_factor, void *stream);

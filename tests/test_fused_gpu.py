@@ -65,3 +65,15 @@ def test_general_factors_odd_extents_and_rank4(cuda):
 def test_shared_source(cuda):
     perms = [TRIPLES_SORTACC6[0][0]] * 3 + list(TRIPLES_SORTACC6[0][1:4])
     run_group(cuda, (10, 12, 8, 10, 12, 8), perms, [1.0, -1.0, 0.5, 1.0, 1.0, -1.0], 800, share=True)
+
+
+@pytest.mark.parametrize("group", [0, 2])
+def test_triples_partial_boxes(cuda, group):
+    """Shapes whose TMA boxes (16 along the sources' stride-1 dim, up to 64
+    along the output's) end in partial boxes, and an odd extent that sends
+    some passes to the cp.async kernel."""
+    perms = TRIPLES_SORTACC6[group]
+    rnd = random.Random(40 + group)
+    factors = [rnd.choice([1.0, -1.0, 0.5]) for _ in perms]
+    run_group(cuda, (20, 12, 18, 20, 12, 18), perms, factors, 900 + group)
+    run_group(cuda, (18, 6, 20, 18, 6, 19), perms, factors, 950 + group)
