@@ -179,14 +179,15 @@ spg_fused_sortacc(double *__restrict__ out, const __grid_constant__ FusedParams 
 }
 
 // ===========================================================================
-// TMA-staged form of one pass.  The box spans two output dims: the one the
-// pass's sources hold stride-1 (p, 16 elements) and the output's stride-1
-// dim (q, lq elements); every other dim has box length 1.  Every source
-// tile then has the same layout, [p fastest (16 doubles = one 128-byte
-// row), q], so one index per element serves every source; the tiles are
-// loaded with the 128-byte swizzle, which spreads the q-strided reads of a
-// warp over the banks.  The old output tile and the result are in output
-// order, [q fastest, p].
+// TMA-staged form of one pass.  The box spans three output dims: the one
+// the pass's sources hold stride-1 (p, 16 elements), the output's stride-1
+// dim (q, lq elements) and one more (r, lr elements); every other dim has
+// box length 1.  Every source tile then has the layout [p fastest (16
+// doubles = one 128-byte row), then q and r in the source's order], so two
+// precomputed indices per element (q before r, or r before q) serve every
+// source; the tiles are loaded with the 128-byte swizzle, which spreads the
+// row-strided reads of a warp over the banks.  The old output tile and the
+// result are in output order, [q fastest, then p and r].
 //
 // Warp-specialised like spg_tiled_tma: a load thread streams the items of
 // each box (old output tile, then source 0..nsrc-1) through a ring of S
@@ -202,7 +203,9 @@ struct FusedTmaParams {
     FastDiv gcnt[SPG_FUSED_MAXR];
     int8_t mdim[SPG_FT_MAXS + 1][SPG_FUSED_MAXR];  // per map (0 = output) and grid dim
     int32_t mul[SPG_FT_MAXS + 1][SPG_FUSED_MAXR];  // map coordinate step per box
-    int32_t nsrc, vol, lq;
+    int32_t nsrc, vol, lq, lr;                     // box: 16 along p, lq along q, lr along r
+    int32_t out_r_first;                           // output order lists r before p
+    int32_t src_r_first[SPG_FT_MAXS];              // source k lists r before q
     uint32_t tile_bytes;                           // one slot, 1024-aligned
     uint32_t tx;                                   // bytes one load delivers
     SpgFactor fac[SPG_FT_MAXS];
@@ -264,15 +267,20 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
     // permute threads: output-order element e = tid + m*NT of the box is
     // (xq, xp) = (e % lq, e / lq); its byte offset in a (swizzled) source
     // tile is ((xp + 16*xq) * 8) with the 16-byte chunk index XOR row % 8
-    uint32_t soff[EPT];
+    uint32_t soff[EPT], soff_r[EPT];       // q-before-r and r-before-q sources
 #pragma unroll
     for (int m = 0; m < EPT; ++m) {
         const uint32_t e = tid + (uint32_t)m * NT;
         soff[m] = 0xFFFFFFFFu;
+        soff_r[m] = 0xFFFFFFFFu;
         if (tid < NT && e < (uint32_t)p.vol) {
-            const uint32_t xq = e % (uint32_t)p.lq, xp = e / (uint32_t)p.lq;
-            const uint32_t o = (xp + 16u * xq) * 8u;
-            soff[m] = o ^ ((xq & 7u) << 4);
+            const uint32_t lq = (uint32_t)p.lq, lr = (uint32_t)p.lr;
+            const uint32_t xq = e % lq, rest = e / lq;
+            const uint32_t xp = p.out_r_first ? rest / lr : rest % 16u;
+            const uint32_t xr = p.out_r_first ? rest % lr : rest / 16u;
+            const uint32_t row_a = xq + lq * xr, row_b = xr + lr * xq;   // 128-byte rows
+            soff[m] = ((xp + 16u * row_a) * 8u) ^ ((row_a & 7u) << 4);
+            soff_r[m] = ((xp + 16u * row_b) * 8u) ^ ((row_b & 7u) << 4);
         }
     }
     __syncthreads();                        // barriers initialised before anyone waits
@@ -344,10 +352,12 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
             } else {
                 const SpgFactor F = p.fac[i - 1];
                 const int op = p.op[i - 1];
+                const bool rf = p.src_r_first[i - 1] != 0;
 #pragma unroll
                 for (int m = 0; m < EPT; ++m)
                     if (soff[m] != 0xFFFFFFFFu)
-                        acc[m] = spg_fused_apply(op, acc[m], *reinterpret_cast<const double *>(slot + soff[m]), F);
+                        acc[m] = spg_fused_apply(op, acc[m],
+                                                 *reinterpret_cast<const double *>(slot + (rf ? soff_r[m] : soff[m])), F);
             }
             __syncwarp();
             if (lane == 0) spg_mbar_arrive(empty0 + 8u * (uint32_t)s);
@@ -488,6 +498,11 @@ static bool ft_map(int R, const int *order, const int64_t *ext, const int64_t *s
     return true;
 }
 
+static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
+                         int nsrc, const double *const *unsorted, const double *factors, double *sorted,
+                         void *stream, int p, int q, int r, const int64_t *L, FusedTmaParams *PP,
+                         FusedTmaMaps *MM, bool launch);
+
 // The TMA-staged pass, or SPAGHETTY_ERR_NOKERNEL when the shapes or the
 // buffers do not allow it (the caller then runs the cp.async kernel).
 // O, ostr: kept output dims (output order) and their element strides;
@@ -509,14 +524,48 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
     if (p < 0 || p == q || O[p] < 16 || O[q] < 8) return SPAGHETTY_ERR_NOKERNEL;
     int64_t lq = std::min<int64_t>(O[q], 64);
     lq &= ~(int64_t)1;
-    int64_t L[SPG_FUSED_MAXR];
-    for (int i = 0; i < R; ++i) L[i] = 1;
-    L[p] = 16;
-    L[q] = lq;
-    const int64_t vol = 16 * lq;
-    if (vol > SPG_FT_NT * SPG_FT_EPT) return SPAGHETTY_ERR_NOKERNEL;
     static thread_local FusedTmaParams P;
     static thread_local FusedTmaMaps M;
+    // the third box dim r: the first (in output order, fastest first) whose
+    // box keeps every map within five dims; lr fills the CTA's elements
+    const int64_t cap = SPG_FT_NT * SPG_FT_EPT;
+    int best_r = -2;
+    int64_t best_vol = 0, bestL[SPG_FUSED_MAXR];
+    for (int r = -1; r < R; ++r) {          // -1: a two-dim box
+        if (r == p || r == q) continue;
+        int64_t L[SPG_FUSED_MAXR];
+        for (int i = 0; i < R; ++i) L[i] = 1;
+        L[p] = 16;
+        L[q] = lq;
+        if (r >= 0) {
+            L[r] = std::min<int64_t>(O[r], cap / (16 * lq));
+            if (L[r] < 2) continue;
+        }
+        const int64_t vol = 16 * lq * (r >= 0 ? L[r] : 1);
+        if (vol <= best_vol) continue;
+        if (fused_tma_try(R, O, ostr, sstr, nsrc, unsorted, factors, sorted, stream, p, q, r < 0 ? p : r, L,
+                          &P, &M, false) != SPAGHETTY_OK)
+            continue;
+        best_r = r;
+        best_vol = vol;
+        std::memcpy(bestL, L, sizeof(L));
+    }
+    if (best_r == -2) return SPAGHETTY_ERR_NOKERNEL;
+    return fused_tma_try(R, O, ostr, sstr, nsrc, unsorted, factors, sorted, stream, p, q,
+                         best_r < 0 ? p : best_r, bestL, &P, &M, true);
+}
+
+// One attempt at the TMA-staged pass with box L (16 along p, lq along q,
+// lr along r; r == p for a two-dim box).
+static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
+                         int nsrc, const double *const *unsorted, const double *factors, double *sorted,
+                         void *stream, int p, int q, int r, const int64_t *L, FusedTmaParams *PP,
+                         FusedTmaMaps *MM, bool launch) {
+    FusedTmaParams &P = *PP;
+    FusedTmaMaps &M = *MM;
+    const int64_t lq = L[q], lr = r == p ? 1 : L[r];
+    const int64_t vol = 16 * lq * lr;
+    if (vol > SPG_FT_NT * SPG_FT_EPT) return SPAGHETTY_ERR_NOKERNEL;
     std::memset(&P, 0, sizeof(P));
     // grid: kept dims with more than one box, output order fastest first
     int gd[SPG_FUSED_MAXR];
@@ -558,6 +607,11 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
     P.nsrc = nsrc;
     P.vol = (int32_t)vol;
     P.lq = (int32_t)lq;
+    P.lr = (int32_t)lr;
+    // output order (fastest first) is q, then p and r as their strides say;
+    // a source lists q before r when q's stride there is the smaller
+    P.out_r_first = (r != p && ostr[r] < ostr[p]) ? 1 : 0;
+    for (int k = 0; k < nsrc; ++k) P.src_r_first[k] = (r != p && sstr[k][r] < sstr[k][q]) ? 1 : 0;
     P.tile_bytes = (uint32_t)(((vol * 8) + 1023) & ~(int64_t)1023);
     P.tx = (uint32_t)(vol * 8);
     for (int k = 0; k < nsrc; ++k) {
@@ -565,6 +619,7 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
         P.op[k] = spg_choose_op(factors[k], 1.0);
     }
     P.status = spg_status_word();
+    if (!launch) return SPAGHETTY_OK;
     const size_t smem = (size_t)(SPG_FT_S + 2) * P.tile_bytes + (2 * SPG_FT_S + 4) * 8 + 1024;
     const void *fn = (const void *)spg_fused_tma<SPG_FT_NT, SPG_FT_EPT, SPG_FT_S>;
     if (smem > 48 * 1024 && cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess) {
