@@ -203,11 +203,13 @@ struct FusedTmaParams {
     FastDiv gcnt[SPG_FUSED_MAXR];
     int8_t mdim[SPG_FT_MAXS + 1][SPG_FUSED_MAXR];  // per map (0 = output) and grid dim
     int32_t mul[SPG_FT_MAXS + 1][SPG_FUSED_MAXR];  // map coordinate step per box
-    int32_t nsrc, vol, lq, lr;                     // box: 16 along p, lq along q, lr along r
+    int32_t nsrc, vol, lq, lr, lp;                 // output box: lp along p, lq along q, lr along r
+    int32_t pw;                                    // source tile row: pw doubles along p
+    int32_t swz;                                   // 1: 128-byte swizzled source rows (pw == 16)
     int32_t out_r_first;                           // output order lists r before p
     int32_t src_r_first[SPG_FT_MAXS];              // source k lists r before q
     uint32_t tile_bytes;                           // one slot, 1024-aligned
-    uint32_t tx;                                   // bytes one load delivers
+    uint32_t tx_out, tx_src;                       // bytes one load delivers
     SpgFactor fac[SPG_FT_MAXS];
     int32_t op[SPG_FT_MAXS];
     int *status;
@@ -274,13 +276,18 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
         soff[m] = 0xFFFFFFFFu;
         soff_r[m] = 0xFFFFFFFFu;
         if (tid < NT && e < (uint32_t)p.vol) {
-            const uint32_t lq = (uint32_t)p.lq, lr = (uint32_t)p.lr;
+            const uint32_t lq = (uint32_t)p.lq, lr = (uint32_t)p.lr, lp = (uint32_t)p.lp;
+            const uint32_t pw = (uint32_t)p.pw;
             const uint32_t xq = e % lq, rest = e / lq;
-            const uint32_t xp = p.out_r_first ? rest / lr : rest % 16u;
-            const uint32_t xr = p.out_r_first ? rest % lr : rest / 16u;
-            const uint32_t row_a = xq + lq * xr, row_b = xr + lr * xq;   // 128-byte rows
-            soff[m] = ((xp + 16u * row_a) * 8u) ^ ((row_a & 7u) << 4);
-            soff_r[m] = ((xp + 16u * row_b) * 8u) ^ ((row_b & 7u) << 4);
+            const uint32_t xp = p.out_r_first ? rest / lr : rest % lp;
+            const uint32_t xr = p.out_r_first ? rest % lr : rest / lp;
+            const uint32_t row_a = xq + lq * xr, row_b = xr + lr * xq;   // source tile rows
+            soff[m] = (xp + pw * row_a) * 8u;
+            soff_r[m] = (xp + pw * row_b) * 8u;
+            if (p.swz) {                    // 16-byte chunk index XOR row % 8
+                soff[m] ^= (row_a & 7u) << 4;
+                soff_r[m] ^= (row_b & 7u) << 4;
+            }
         }
     }
     __syncthreads();                        // barriers initialised before anyone waits
@@ -300,7 +307,7 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
                 int32_t c[5];
                 spg_ft_coords(p, i, t, c);
                 const uint32_t mb = full0 + 8u * (uint32_t)s;
-                spg_mbar_expect_tx(mb, p.tx);
+                spg_mbar_expect_tx(mb, i == 0 ? p.tx_out : p.tx_src);
                 spg_tma_load5(base + (uint32_t)s * tb, &maps.m[i], c, mb);
             }
         }
@@ -346,18 +353,20 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
                 const double *told = reinterpret_cast<const double *>(slot);
 #pragma unroll
                 for (int m = 0; m < EPT; ++m) {
-                    const uint32_t e = tid + (uint32_t)m * NT;
-                    acc[m] = soff[m] != 0xFFFFFFFFu ? told[e] : 0.0;
+                    acc[m] = 0.0;
+                    if (soff[m] == 0xFFFFFFFFu) break;   // the rest of this thread's slots are empty
+                    acc[m] = told[tid + (uint32_t)m * NT];
                 }
             } else {
                 const SpgFactor F = p.fac[i - 1];
                 const int op = p.op[i - 1];
                 const bool rf = p.src_r_first[i - 1] != 0;
 #pragma unroll
-                for (int m = 0; m < EPT; ++m)
-                    if (soff[m] != 0xFFFFFFFFu)
-                        acc[m] = spg_fused_apply(op, acc[m],
-                                                 *reinterpret_cast<const double *>(slot + (rf ? soff_r[m] : soff[m])), F);
+                for (int m = 0; m < EPT; ++m) {
+                    if (soff[m] == 0xFFFFFFFFu) break;
+                    acc[m] = spg_fused_apply(op, acc[m],
+                                             *reinterpret_cast<const double *>(slot + (rf ? soff_r[m] : soff[m])), F);
+                }
             }
             __syncwarp();
             if (lane == 0) spg_mbar_arrive(empty0 + 8u * (uint32_t)s);
@@ -369,8 +378,8 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
         double *tout = reinterpret_cast<double *>(smem + out0 + (size_t)o * tb);
 #pragma unroll
         for (int m = 0; m < EPT; ++m) {
-            const uint32_t e = tid + (uint32_t)m * NT;
-            if (soff[m] != 0xFFFFFFFFu) tout[e] = acc[m];
+            if (soff[m] == 0xFFFFFFFFu) break;
+            tout[tid + (uint32_t)m * NT] = acc[m];
         }
         spg_fence_async_smem();
         __syncwarp();
@@ -500,8 +509,11 @@ static bool ft_map(int R, const int *order, const int64_t *ext, const int64_t *s
 
 static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
                          int nsrc, const double *const *unsorted, const double *factors, double *sorted,
-                         void *stream, int p, int q, int r, const int64_t *L, FusedTmaParams *PP,
-                         FusedTmaMaps *MM, bool launch);
+                         void *stream, int p, int q, int r, const int64_t *L, int64_t pw,
+                         FusedTmaParams *PP, FusedTmaMaps *MM, bool launch);
+static int fused_tma_mode(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
+                          int nsrc, const double *const *unsorted, const double *factors, double *sorted,
+                          void *stream, int p, int q, int64_t lq, int64_t lp, int64_t pw);
 
 // The TMA-staged pass, or SPAGHETTY_ERR_NOKERNEL when the shapes or the
 // buffers do not allow it (the caller then runs the cp.async kernel).
@@ -524,10 +536,35 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
     if (p < 0 || p == q || O[p] < 16 || O[q] < 8) return SPAGHETTY_ERR_NOKERNEL;
     int64_t lq = std::min<int64_t>(O[q], 64);
     lq &= ~(int64_t)1;
+    // source tiles: the whole of p in one row of pw doubles, pw the
+    // smallest even width >= O[p] with pw/2 odd (rows of an odd number of
+    // 16-byte chunks spread a warp's row-strided reads over the banks; the
+    // columns past O[p] are out of the tensor, zero-filled, never read from
+    // memory), or, for long p, rows of 16 doubles with the 128-byte swizzle
+    for (int mode = O[p] <= 64 ? 0 : 1; mode < 2; ++mode) {
+        int64_t lp = 16, pw = 16;
+        if (mode == 0) {
+            lp = O[p];
+            pw = (O[p] + 1) & ~(int64_t)1;
+            if ((pw / 2) % 2 == 0) pw += 2;
+        }
+        const int rc = fused_tma_mode(R, O, ostr, sstr, nsrc, unsorted, factors, sorted, stream, p, q, lq,
+                                      lp, pw);
+        if (rc != SPAGHETTY_ERR_NOKERNEL) return rc;
+    }
+    return SPAGHETTY_ERR_NOKERNEL;
+}
+
+// The TMA-staged pass with source rows of pw doubles along p (lp of them
+// in the output box): the third box dim r that gives the largest box whose
+// maps fit, then the launch.
+static int fused_tma_mode(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
+                          int nsrc, const double *const *unsorted, const double *factors, double *sorted,
+                          void *stream, int p, int q, int64_t lq, int64_t lp, int64_t pw) {
     static thread_local FusedTmaParams P;
     static thread_local FusedTmaMaps M;
-    // the third box dim r: the first (in output order, fastest first) whose
-    // box keeps every map within five dims; lr fills the CTA's elements
+    // the third box dim r: the one giving the largest box whose maps stay
+    // within five dims; its length fills the CTA's elements
     const int64_t cap = SPG_FT_NT * SPG_FT_EPT;
     int best_r = -2;
     int64_t best_vol = 0, bestL[SPG_FUSED_MAXR];
@@ -535,16 +572,16 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
         if (r == p || r == q) continue;
         int64_t L[SPG_FUSED_MAXR];
         for (int i = 0; i < R; ++i) L[i] = 1;
-        L[p] = 16;
+        L[p] = lp;
         L[q] = lq;
         if (r >= 0) {
-            L[r] = std::min<int64_t>(O[r], cap / (16 * lq));
+            L[r] = std::min<int64_t>(O[r], cap / (std::max(lp, pw) * lq));
             if (L[r] < 2) continue;
         }
-        const int64_t vol = 16 * lq * (r >= 0 ? L[r] : 1);
+        const int64_t vol = lp * lq * (r >= 0 ? L[r] : 1);
         if (vol <= best_vol) continue;
         if (fused_tma_try(R, O, ostr, sstr, nsrc, unsorted, factors, sorted, stream, p, q, r < 0 ? p : r, L,
-                          &P, &M, false) != SPAGHETTY_OK)
+                          pw, &P, &M, false) != SPAGHETTY_OK)
             continue;
         best_r = r;
         best_vol = vol;
@@ -552,20 +589,25 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
     }
     if (best_r == -2) return SPAGHETTY_ERR_NOKERNEL;
     return fused_tma_try(R, O, ostr, sstr, nsrc, unsorted, factors, sorted, stream, p, q,
-                         best_r < 0 ? p : best_r, bestL, &P, &M, true);
+                         best_r < 0 ? p : best_r, bestL, pw, &P, &M, true);
 }
 
 // One attempt at the TMA-staged pass with box L (16 along p, lq along q,
 // lr along r; r == p for a two-dim box).
 static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
                          int nsrc, const double *const *unsorted, const double *factors, double *sorted,
-                         void *stream, int p, int q, int r, const int64_t *L, FusedTmaParams *PP,
-                         FusedTmaMaps *MM, bool launch) {
+                         void *stream, int p, int q, int r, const int64_t *L, int64_t pw,
+                         FusedTmaParams *PP, FusedTmaMaps *MM, bool launch) {
     FusedTmaParams &P = *PP;
     FusedTmaMaps &M = *MM;
-    const int64_t lq = L[q], lr = r == p ? 1 : L[r];
-    const int64_t vol = 16 * lq * lr;
-    if (vol > SPG_FT_NT * SPG_FT_EPT) return SPAGHETTY_ERR_NOKERNEL;
+    const int64_t lq = L[q], lr = r == p ? 1 : L[r], lp = L[p];
+    const int64_t vol = lp * lq * lr, vol_src = pw * lq * lr;
+    const bool swz = pw == 16 && lp == 16;
+    if (vol > SPG_FT_NT * SPG_FT_EPT || pw < lp || pw > 256) return SPAGHETTY_ERR_NOKERNEL;
+    // the source maps' box: pw along p (the rest as the output's)
+    int64_t Ls[SPG_FUSED_MAXR];
+    for (int i = 0; i < R; ++i) Ls[i] = L[i];
+    Ls[p] = pw;
     std::memset(&P, 0, sizeof(P));
     // grid: kept dims with more than one box, output order fastest first
     int gd[SPG_FUSED_MAXR];
@@ -592,8 +634,9 @@ static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (
         uint32_t box[5];
         int8_t mdim[SPG_FUSED_MAXR];
         int64_t w[SPG_FUSED_MAXR];
-        if (!ft_map(R, order, O, str, L, mi > 0, dim, stride, box, mdim, w)) return SPAGHETTY_ERR_NOKERNEL;
-        if (mi > 0 && box[0] != 16) return SPAGHETTY_ERR_NOKERNEL;   // one 128-byte swizzled row
+        if (!ft_map(R, order, O, str, mi > 0 ? Ls : L, mi > 0, dim, stride, box, mdim, w))
+            return SPAGHETTY_ERR_NOKERNEL;
+        if (mi > 0 && box[0] != (uint32_t)pw) return SPAGHETTY_ERR_NOKERNEL;   // one source row
         for (int g = 0; g < ng; ++g) {
             const int i = gd[g];
             const int64_t mul = L[i] * w[i];
@@ -602,18 +645,23 @@ static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (
             P.mul[mi][g] = (int32_t)mul;
         }
         const double *ptr = mi == 0 ? sorted : unsorted[mi - 1];
-        if (spg_encode_map(&M.m[mi], ptr, dim, stride, box, mi > 0) != SPAGHETTY_OK) return SPAGHETTY_ERR_NOKERNEL;
+        if (spg_encode_map(&M.m[mi], ptr, dim, stride, box, mi > 0 && swz) != SPAGHETTY_OK)
+            return SPAGHETTY_ERR_NOKERNEL;
     }
     P.nsrc = nsrc;
     P.vol = (int32_t)vol;
     P.lq = (int32_t)lq;
     P.lr = (int32_t)lr;
+    P.lp = (int32_t)lp;
+    P.pw = (int32_t)pw;
+    P.swz = swz ? 1 : 0;
     // output order (fastest first) is q, then p and r as their strides say;
     // a source lists q before r when q's stride there is the smaller
     P.out_r_first = (r != p && ostr[r] < ostr[p]) ? 1 : 0;
     for (int k = 0; k < nsrc; ++k) P.src_r_first[k] = (r != p && sstr[k][r] < sstr[k][q]) ? 1 : 0;
-    P.tile_bytes = (uint32_t)(((vol * 8) + 1023) & ~(int64_t)1023);
-    P.tx = (uint32_t)(vol * 8);
+    P.tile_bytes = (uint32_t)(((std::max(vol, vol_src) * 8) + 1023) & ~(int64_t)1023);
+    P.tx_out = (uint32_t)(vol * 8);
+    P.tx_src = (uint32_t)(vol_src * 8);
     for (int k = 0; k < nsrc; ++k) {
         P.fac[k] = spg_make_factor(factors[k], 1.0);
         P.op[k] = spg_choose_op(factors[k], 1.0);
