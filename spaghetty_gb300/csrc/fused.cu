@@ -536,12 +536,14 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
     if (p < 0 || p == q || O[p] < 16 || O[q] < 8) return SPAGHETTY_ERR_NOKERNEL;
     int64_t lq = std::min<int64_t>(O[q], 64);
     lq &= ~(int64_t)1;
-    // source tiles: the whole of p in one row of pw doubles, pw the
-    // smallest even width >= O[p] with pw/2 odd (rows of an odd number of
-    // 16-byte chunks spread a warp's row-strided reads over the banks; the
-    // columns past O[p] are out of the tensor, zero-filled, never read from
-    // memory), or, for long p, rows of 16 doubles with the 128-byte swizzle
-    for (int mode = O[p] <= 64 ? 0 : 1; mode < 2; ++mode) {
+    // source tiles: rows of 16 doubles along p with the 128-byte swizzle,
+    // or the whole of a short p in one row of pw doubles, pw the smallest
+    // even width >= O[p] with pw/2 odd (rows of an odd number of 16-byte
+    // chunks spread a warp's row-strided reads over the banks; the columns
+    // past O[p] are out of the tensor, zero-filled, never read from memory)
+    // extents that 16 divides keep whole swizzled rows; other short ones
+    // are loaded whole into padded rows
+    for (int mode = (O[p] <= 64 && O[p] % 16 != 0) ? 0 : 1; mode < 2; ++mode) {
         int64_t lp = 16, pw = 16;
         if (mode == 0) {
             lp = O[p];
