@@ -18,6 +18,7 @@ that behaviour).
 from __future__ import annotations
 
 import ctypes
+import math
 from typing import Sequence
 
 import numpy as np
@@ -54,6 +55,29 @@ def _numel(x) -> int:
     return int(x.numel()) if (torch is not None and isinstance(x, torch.Tensor)) else int(x.size)
 
 
+# ctypes int arrays of the (dims, perm) tuples seen so far: building them is
+# a large part of a small call's host time
+_ARRAYS: dict = {}
+
+
+def _int_array_cached(vals):
+    key = tuple(int(v) for v in vals)
+    a = _ARRAYS.get(key)
+    if a is None:
+        if len(_ARRAYS) > 4096:
+            _ARRAYS.clear()
+        a = _ARRAYS[key] = int_array(key)
+    return a
+
+
+def _raw_stream(dev_index: int) -> int:
+    """torch's current stream on the device, as a cudaStream_t value."""
+    get = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+    if get is not None:
+        return int(get(dev_index))
+    return int(torch.cuda.current_stream(dev_index).cuda_stream)
+
+
 def sort_generic(unsorted, sorted, dims: Sequence[int], perm: Sequence[int],
                  factor: float, acc_factor: float = 0.0, stream=None) -> None:
     """Two-factor form of the generated nests (trunk/generator2.py:57-130):
@@ -61,24 +85,19 @@ def sort_generic(unsorted, sorted, dims: Sequence[int], perm: Sequence[int],
     rank = len(dims)
     if len(perm) != rank:
         raise ValueError("dims and perm differ in length")
-    n = int(np.prod([int(d) for d in dims])) if rank else 0
+    n = math.prod(int(d) for d in dims) if rank else 0
     for t in (unsorted, sorted):
         if _numel(t) != n:
             raise ValueError("buffer holds %d elements, dims need %d" % (_numel(t), n))
-    d = int_array(dims)
-    p = int_array(perm)
+    d = _int_array_cached(dims)
+    p = _int_array_cached(perm)
     L = lib()
     if _is_cuda_tensor(unsorted) and _is_cuda_tensor(sorted):
-        dev = unsorted.device.index
+        # the library runs on the device that holds the tensors
         if stream is None:
-            stream = torch.cuda.current_stream(dev).cuda_stream
-        args = (rank, _ptr(unsorted), _ptr(sorted), d, p, float(factor), float(acc_factor),
-                ctypes.c_void_p(int(stream)))
-        if dev == torch.cuda.current_device():
-            rc = L.spaghetty_sort_async(*args)
-        else:
-            with torch.cuda.device(dev):
-                rc = L.spaghetty_sort_async(*args)
+            stream = _raw_stream(unsorted.device.index)
+        rc = L.spaghetty_sort_async(rank, _ptr(unsorted), _ptr(sorted), d, p, float(factor),
+                                    float(acc_factor), ctypes.c_void_p(int(stream)))
     else:
         if _is_cuda_tensor(unsorted) or _is_cuda_tensor(sorted):
             torch.cuda.current_stream().synchronize()
