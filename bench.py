@@ -529,7 +529,8 @@ def run_batched(args, dev, ext4=(8, 40), ext6=(6, 20), n=4096, seed=2024):
            "work_units": info["units"], "bytes_per_launch": total_b,
            "persistent_graph": {"tiles_per_s": round(n / t_graph, 1),
                                 "gbs": round(total_b / t_graph / 1e9, 1),
-                                "ms": round(t_graph * 1e3, 3), "launches": 1},
+                                "ms": round(t_graph * 1e3, 3), "launches": info["launches"],
+                                "sorts_on_work_list": info["jobs"]},
            "one_launch_per_tile": {"tiles_per_s": round(n / t_plain, 1),
                                    "gbs": round(total_b / t_plain / 1e9, 1),
                                    "ms": round(t_plain * 1e3, 3), "launches": n},

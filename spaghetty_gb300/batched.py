@@ -55,7 +55,8 @@ class Batch:
     def info(self) -> dict:
         v = (ctypes.c_int64 * 4)()
         check(lib().spaghetty_batch_info(self._h, v), "batch info")
-        return {"jobs": v[0], "units": v[1], "bytes": v[2], "smem_bytes": v[3]}
+        return {"jobs": v[0], "units": v[1], "bytes": v[2], "smem_bytes": v[3],
+                "launches": int(lib().spaghetty_batch_launches(self._h))}
 
     def _stream(self, stream):
         if stream is None:
@@ -63,7 +64,8 @@ class Batch:
         return ctypes.c_void_p(int(stream))
 
     def launch(self, stream=None) -> None:
-        """Enqueue every sort as ONE persistent kernel launch."""
+        """Enqueue the batch: the sorts of at least 2^20 elements one launch
+        each, every other sort in ONE persistent kernel launch."""
         check(lib().spaghetty_batch_launch(self._h, self._stream(stream)), "batch launch")
 
     def launch_plain(self, stream=None) -> None:

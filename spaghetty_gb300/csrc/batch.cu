@@ -30,6 +30,12 @@
 #define SPG_BATCH_EPT 4
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
 #define SPG_BATCH_UNIT_ELEMS 16384
+// Sorts of at least this many elements fill the GPU by themselves: a batch
+// launch runs each of them with its own tuned single-sort plan (the
+// TMA-staged kernel where it applies), then the persistent kernel over the
+// rest.  Both are enqueued on the same stream, so a captured graph holds
+// them all.
+#define SPG_BATCH_DIRECT_ELEMS (1 << 20)
 #define SPG_BATCH_S 4          // cp.async stages of the tiled path
 
 struct BatchJob {
@@ -209,6 +215,7 @@ struct spaghetty_batch {
     uint32_t *d_words = nullptr;      // [0] = unit counter, [1] = status word
     std::vector<spaghetty_batch_entry> entries;
     std::vector<BatchJob> jobs;       // host copy of the job records
+    std::vector<int> direct;          // entries large enough to run as their own launch
     int64_t bytes = 0;                // algorithmic bytes of one launch
 };
 
@@ -297,6 +304,12 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         const uintptr_t nb = (uintptr_t)fo.nelem * sizeof(double);
         ranges.push_back({(uintptr_t)e.unsorted, (uintptr_t)e.unsorted + nb, i, false});
         ranges.push_back({(uintptr_t)e.sorted, (uintptr_t)e.sorted + nb, i, true});
+        if (fo.nelem >= SPG_BATCH_DIRECT_ELEMS) {
+            const int op = spg_choose_op(e.factor, e.acc_factor);
+            b->direct.push_back(i);
+            b->bytes += fo.nelem * (spg_op_class(op) == 0 ? 16 : 24);
+            continue;
+        }
         Plan pl;
         const int op = spg_choose_op(e.factor, e.acc_factor);
         SpgBatchRule rule;
@@ -395,6 +408,23 @@ int spaghetty_batch_tune_set(int rank, int ext_lo, int ext_hi, int run_in, int r
 int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
     if (!b) return SPAGHETTY_ERR_NULL;
     cudaStream_t st = (cudaStream_t)stream;
+    if (!b->direct.empty()) {
+        int cur = -1;
+        if (cudaGetDevice(&cur) != cudaSuccess) cudaGetLastError();
+        if (cudaSetDevice(b->dev) != cudaSuccess) {
+            cudaGetLastError();
+            return SPAGHETTY_ERR_CUDA;
+        }
+        int rc = SPAGHETTY_OK;
+        for (int i : b->direct) {
+            const spaghetty_batch_entry &e = b->entries[(size_t)i];
+            rc = spg_sort_async_on(b->dev, e.rank, e.unsorted, e.sorted, e.dims, e.perm, e.factor,
+                                   e.acc_factor, stream);
+            if (rc) break;
+        }
+        if (cur >= 0 && cur != b->dev) cudaSetDevice(cur);
+        if (rc) return rc;
+    }
     if (b->total_units == 0) return SPAGHETTY_OK;
     if (cudaMemsetAsync(b->d_words, 0, sizeof(uint32_t), st) != cudaSuccess) {
         cudaGetLastError();
@@ -451,6 +481,11 @@ int spaghetty_batch_status(spaghetty_batch *b, void *stream) {
         return SPAGHETTY_ERR_CUDA;
     }
     return st ? SPAGHETTY_ERR_DEVICE : SPAGHETTY_OK;
+}
+
+int spaghetty_batch_launches(const spaghetty_batch *b) {
+    if (!b) return -SPAGHETTY_ERR_NULL;
+    return (int)b->direct.size() + (b->total_units > 0 ? 1 : 0);
 }
 
 int spaghetty_batch_info(const spaghetty_batch *b, int64_t *info) {

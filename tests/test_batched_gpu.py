@@ -183,3 +183,26 @@ def test_size_bucket_rules(cuda, rule):
         got = ds.cpu().numpy()
         want = expect(sp, u, y, g)
         assert bits_equal(got, want), (sp, rule, first_mismatch(got, want))
+
+
+def test_large_sorts_run_as_their_own_launches(cuda):
+    """Sorts of at least 2^20 elements leave the work list and run their own
+    single-sort plans inside the same launch (and the same captured graph);
+    every sort still matches the oracle."""
+    from spaghetty_gb300.batched import Batch
+    specs = small_specs(40, 9)
+    big = [{"dims": (64, 40, 20, 24), "perm": (4, 2, 1, 3), "factor": -0.5, "g": 0.0},
+           {"dims": (12, 10, 12, 10, 8, 12), "perm": (3, 2, 6, 1, 5, 4), "factor": 1.0, "g": 1.0},
+           {"dims": (40, 64, 24, 20), "perm": (1, 3, 2, 4), "factor": 0.75, "g": -0.25}]
+    specs = specs[:20] + big + specs[20:]
+    jobs, host = make_jobs(specs, cuda, 400)
+    b = Batch(jobs)
+    info = b.info()
+    assert info["jobs"] == 40 and info["launches"] == 4
+    b.capture()          # warm-up launch, then capture
+    b.replay()           # the sorts ran twice: sortaccs accumulate twice
+    assert b.status() == 0
+    for sp, (du, ds, *_), (u, y, g) in zip(specs, jobs, host):
+        got = ds.cpu().numpy()
+        want = expect(sp, u, y, g, times=2)
+        assert bits_equal(got, want), (sp, first_mismatch(got, want))
