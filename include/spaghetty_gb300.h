@@ -340,9 +340,10 @@ typedef struct spaghetty_batch spaghetty_batch;
 int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghetty_batch **out);
 int spaghetty_batch_bad_index(void);
 
-/* Enqueue the whole batch on `stream`: the sorts of at least 2^20 elements
- * one launch each, then a counter reset and ONE persistent kernel launch
- * over the rest.  Capturable in a CUDA graph. */
+/* Enqueue the whole batch on `stream`: the sorts of at least 2^22 elements
+ * that the single-sort planner puts on the TMA-staged kernel one launch
+ * each, then a counter reset and ONE persistent kernel launch over the
+ * rest.  Capturable in a CUDA graph. */
 int spaghetty_batch_launch(spaghetty_batch *batch, void *stream);
 
 /* The same sorts as one launch each through spaghetty_sort_async (the plain
@@ -358,9 +359,9 @@ int spaghetty_batch_status(spaghetty_batch *batch, void *stream);
  * bytes per CTA}. */
 int spaghetty_batch_info(const spaghetty_batch *batch, int64_t *info);
 
-/* Kernel launches one spaghetty_batch_launch enqueues: sorts of at least
- * 2^20 elements run as their own launch (their tuned single-sort plan), the
- * rest as one persistent launch. */
+/* Kernel launches one spaghetty_batch_launch enqueues: the large
+ * TMA-planned sorts run as their own launch, the rest as one persistent
+ * launch. */
 int spaghetty_batch_launches(const spaghetty_batch *batch);
 
 /* Fault injection for tests, done by the host: overwrite job `index`'s kind

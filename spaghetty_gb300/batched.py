@@ -64,8 +64,9 @@ class Batch:
         return ctypes.c_void_p(int(stream))
 
     def launch(self, stream=None) -> None:
-        """Enqueue the batch: the sorts of at least 2^20 elements one launch
-        each, every other sort in ONE persistent kernel launch."""
+        """Enqueue the batch: the large sorts the single-sort planner puts on
+        the TMA-staged kernel one launch each, every other sort in ONE
+        persistent kernel launch."""
         check(lib().spaghetty_batch_launch(self._h, self._stream(stream)), "batch launch")
 
     def launch_plain(self, stream=None) -> None:

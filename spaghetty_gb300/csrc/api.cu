@@ -758,6 +758,16 @@ int *spg_status_word() { return status_word_dev(); }
 // The asynchronous sort for pointers already known to be device memory of
 // device `dev`, the current device of the calling thread (the batched
 // plain path, which validated them when the batch was created).
+// Whether the single-sort plan of this problem on these buffers is the
+// TMA-staged kernel (batch.cu runs such large sorts as their own launch).
+bool spg_plan_is_tma(int dev, int rank, const int *dims, const int *perm, double factor, double acc_factor,
+                     const double *unsorted, const double *sorted) {
+    Plan pl;
+    return make_plan(rank, dims, perm, factor, acc_factor, device_sms(dev), &pl,
+                     aligned16(unsorted) && aligned16(sorted)) == SPAGHETTY_OK &&
+           pl.kind == KIND_TMA;
+}
+
 int spg_sort_async_on(int dev, int rank, const double *unsorted, double *sorted, const int *dims,
                       const int *perm, double factor, double acc_factor, void *stream) {
     Folded fo;

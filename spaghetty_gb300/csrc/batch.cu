@@ -30,12 +30,12 @@
 #define SPG_BATCH_EPT 4
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
 #define SPG_BATCH_UNIT_ELEMS 16384
-// Sorts of at least this many elements fill the GPU by themselves: a batch
-// launch runs each of them with its own tuned single-sort plan (the
-// TMA-staged kernel where it applies), then the persistent kernel over the
-// rest.  Both are enqueued on the same stream, so a captured graph holds
-// them all.
-#define SPG_BATCH_DIRECT_ELEMS (1 << 20)
+// Sorts of at least this many elements whose single-sort plan is the
+// TMA-staged kernel fill the GPU by themselves at a higher rate than the
+// persistent kernel: a batch launch runs each of them as its own launch,
+// then the persistent kernel over the rest.  Both are enqueued on the same
+// stream, so a captured graph holds them all.
+#define SPG_BATCH_DIRECT_ELEMS (1 << 22)
 #define SPG_BATCH_S 4          // cp.async stages of the tiled path
 
 struct BatchJob {
@@ -304,7 +304,8 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         const uintptr_t nb = (uintptr_t)fo.nelem * sizeof(double);
         ranges.push_back({(uintptr_t)e.unsorted, (uintptr_t)e.unsorted + nb, i, false});
         ranges.push_back({(uintptr_t)e.sorted, (uintptr_t)e.sorted + nb, i, true});
-        if (fo.nelem >= SPG_BATCH_DIRECT_ELEMS) {
+        if (fo.nelem >= SPG_BATCH_DIRECT_ELEMS &&
+            spg_plan_is_tma(b->dev, e.rank, e.dims, e.perm, e.factor, e.acc_factor, e.unsorted, e.sorted)) {
             const int op = spg_choose_op(e.factor, e.acc_factor);
             b->direct.push_back(i);
             b->bytes += fo.nelem * (spg_op_class(op) == 0 ? 16 : 24);

@@ -175,6 +175,9 @@ struct CUtensorMap_st;
 int spg_encode_map(CUtensorMap_st *m, const double *ptr, const uint64_t *dim, const uint64_t *stride,
                    const uint32_t *box, int swizzle128);
 int *spg_status_word();
+// Whether the single-sort plan of a problem is the TMA-staged kernel (api.cu).
+bool spg_plan_is_tma(int dev, int rank, const int *dims, const int *perm, double factor, double acc_factor,
+                     const double *unsorted, const double *sorted);
 // Asynchronous sort of device pointers of device `dev` (api.cu), no pointer checks.
 int spg_sort_async_on(int dev, int rank, const double *unsorted, double *sorted, const int *dims,
                       const int *perm, double factor, double acc_factor, void *stream);
