@@ -300,13 +300,6 @@ int spaghetty_tune_load(const char *path);
  * invariant divisors).  Returns 0 when they pass.  Needs no GPU. */
 int spaghetty_selftest(void);
 
-/* On-device check of the integer-pipe double addition the fused kernel uses
- * for part of its sums: n generated operand pairs (every exponent gap,
- * rounding ties, all IEEE classes) added by it and by the FP64 pipe.
- * Returns the number of mismatching results (0), or a negated SPAGHETTY_*
- * code. */
-long long spaghetty_selftest_device(long long n);
-
 /* ---- several sortaccs into one output, fused --------------------------- */
 
 /* For k = 0..nsrc-1 in order: sorted = sorted + factors[k] *

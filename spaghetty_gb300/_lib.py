@@ -114,7 +114,6 @@ PROTOTYPES = {
                                                ctypes.c_void_p]),
     "spaghetty_sort_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "spaghetty_selftest": (ctypes.c_int, []),
-    "spaghetty_selftest_device": (ctypes.c_longlong, [ctypes.c_longlong]),
     "spaghetty_version": (ctypes.c_char_p, []),
 }
 

@@ -24,7 +24,6 @@
 #include "kernels.cuh"
 #include "plan.h"
 #include "tma.cuh"
-#include "arith.cuh"
 
 #include <cuda_runtime.h>
 
@@ -62,21 +61,6 @@ struct FusedParams {
 template <int OPA>
 __device__ __forceinline__ double spg_fused_add(double acc, double x, const SpgFactor &F) {
     return spg_apply<OPA>(x, acc, F);
-}
-
-// acc + f*x with the rounding of a sortacc; INT_ADD: the addition in the
-// integer pipes (spg_dadd_int, bit-identical), to take load off the FP64
-// pipe, which bounds the fused pass.
-template <bool INT_ADD>
-__device__ __forceinline__ double spg_fused_apply2(int op, double acc, double x, const SpgFactor &F) {
-    double p;
-    switch (op) {
-        case OP_ACC_ONE: p = x; break;
-        case OP_ACC_NEG: p = spg_neg(x, F); break;
-        case OP_ACC_POW2: p = spg_pow2(x, F); break;
-        default: p = __dmul_rn(x, F.f); break;
-    }
-    return INT_ADD ? spg_dadd_int(acc, p) : __dadd_rn(acc, p);
 }
 
 __device__ __forceinline__ double spg_fused_apply(int op, double acc, double x, const SpgFactor &F) {
@@ -380,10 +364,8 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
 #pragma unroll
                 for (int m = 0; m < EPT; ++m) {
                     if (soff[m] == 0xFFFFFFFFu) break;
-                    const double x = *reinterpret_cast<const double *>(slot + (rf ? soff_r[m] : soff[m]));
-                    // odd slots add in the integer pipes, even ones in the FP64 pipe
-                    acc[m] = (m & 1) ? spg_fused_apply2<true>(op, acc[m], x, F)
-                                     : spg_fused_apply2<false>(op, acc[m], x, F);
+                    acc[m] = spg_fused_apply(op, acc[m],
+                                             *reinterpret_cast<const double *>(slot + (rf ? soff_r[m] : soff[m])), F);
                 }
             }
             __syncwarp();
