@@ -223,3 +223,33 @@ def test_batch_tune_set_validation():
     assert L.spaghetty_batch_tune_set(4, 16, 8, 16, 32, 512) == 9     # empty range
     assert L.spaghetty_batch_tune_set(4, 8, 16, 0, 32, 512) == 9      # run
     assert L.spaghetty_batch_tune_set(0, 0, 0, 0, 0, 0) == 0          # clear
+
+
+def test_tma_candidates_replay_rank6():
+    """Every TMA candidate the tuner can force for a sample of rank-6 perms
+    (the merges of six folded dims into five map dims) replays correctly."""
+    from spaghetty_gb300.autotune import candidates, clear
+    from spaghetty_gb300.workloads import TRIPLES_SORT6
+    L = lib()
+    rnd = random.Random(11)
+    perms = list(TRIPLES_SORT6[:6]) + [tuple(rnd.sample(range(1, 7), 6)) for _ in range(6)]
+    tried = 0
+    try:
+        for dims in [(4, 6, 4, 6, 4, 6), (6, 4, 8, 2, 6, 4)]:
+            for perm in perms:
+                for op in (0, 1):
+                    _, cands = candidates(dims, perm, op)
+                    for box, nt, ept, st in cands:
+                        if st < 12:
+                            continue
+                        rc = L.spaghetty_tune_set(6, int_array(dims), int_array(perm), op,
+                                                  int_array(box), nt, ept, st)
+                        if rc:
+                            continue
+                        vrc, _ = verify(dims, perm, op)
+                        assert vrc == 0, (dims, perm, op, box, nt, ept, st)
+                        tried += 1
+                    clear()
+    finally:
+        clear()
+    assert tried > 0

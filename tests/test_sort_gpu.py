@@ -403,3 +403,36 @@ def test_async_form_checks_memory_and_binds_device(cuda):
     t.join()
     assert out["rc"] == 0, L.spaghetty_last_cuda_error()
     check(host(s), want, "async sort from a fresh thread")
+
+
+def test_forced_tma_variants_rank6(cuda):
+    """Forced TMA-staged variants of rank-6 sorts (six folded dims merged
+    into five map dims) give the oracle's bits."""
+    from spaghetty_gb300.autotune import candidates, clear
+    L = lib()
+    dims = (4, 6, 4, 6, 4, 6)
+    n = int(np.prod(dims))
+    u = O.seeded_uniform(n, 51)
+    y = O.seeded_uniform(n, 52)
+    du, dy = dev(u, cuda), dev(y, cuda)
+    rnd = random.Random(13)
+    perms = list(TRIPLES_SORT6[:6]) + [tuple(rnd.sample(range(1, 7), 6)) for _ in range(6)]
+    ran = 0
+    try:
+        for perm in perms:
+            for op, f in ((0, 0.5), (1, -1.0)):
+                want = dev(O.np_sort(u, dims, perm, f, float(op), out=y), cuda)
+                _, cands = candidates(dims, perm, op)
+                for box, nt, ept, st in cands:
+                    if st < 12 or L.spaghetty_tune_set(6, int_array(dims), int_array(perm), op,
+                                                       int_array(box), nt, ept, st) != 0:
+                        continue
+                    s = dy.clone()
+                    sort_generic(du, s, dims, perm, f, float(op))
+                    torch.cuda.synchronize()
+                    assert torch.equal(s, want), (perm, op, box, nt, ept, st)
+                    ran += 1
+                clear()
+    finally:
+        clear()
+    assert ran > 0
