@@ -106,6 +106,12 @@ __host__ __device__ __forceinline__ void spg_tma_coords(const KParams &p, const 
     }
 }
 
+// Fetch a tensor map (kernel-parameter space) into the TMA unit's cache
+// ahead of its first use.
+__device__ __forceinline__ void spg_prefetch_tmap(const void *tmap) {
+    asm volatile("prefetch.tensormap [%0];\n" ::"l"(tmap) : "memory");
+}
+
 __device__ __forceinline__ void spg_mbar_arrive(uint32_t addr) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(addr) : "memory");
 }
@@ -152,7 +158,10 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     // permute threads build their tables, so DRAM latency overlaps the
     // prologue
     int issued = 0;                         // load thread: boxes whose loads were issued
+    if (tid == store_tid) spg_prefetch_tmap(&tmap_out);
     if (tid == load_tid) {
+        spg_prefetch_tmap(&tmap_in);
+        if (spg_reads_out<OP>::value) spg_prefetch_tmap(&tmap_out);
 #pragma unroll
         for (int s = 0; s < S; ++s) {
             spg_mbar_init(full0 + 8u * s, 1u);
