@@ -37,6 +37,9 @@
 // stream, so a captured graph holds them all.
 #define SPG_BATCH_DIRECT_ELEMS (1 << 22)
 #define SPG_BATCH_S 4          // cp.async stages of the tiled path
+#ifndef SPG_BATCH_MINB
+#define SPG_BATCH_MINB 1       // CTAs per SM the register allocation must allow
+#endif
 
 struct BatchJob {
     KParams kp;
@@ -133,7 +136,7 @@ __device__ __forceinline__ void spg_batch_units(const BatchJob &j, const SpgTab<
             spg_direct_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(j.kp, tb, j.in, j.out, t);
 }
 
-__global__ void __launch_bounds__(SPG_BATCH_NT)
+__global__ void __launch_bounds__(SPG_BATCH_NT, SPG_BATCH_MINB)
 spg_batched(const BatchJob *__restrict__ jobs, uint32_t njobs,
             const uint32_t *__restrict__ unit_job, uint32_t total_units,
             uint32_t *counter, int *status, int smem_elems) {
