@@ -36,9 +36,11 @@
 // then the persistent kernel over the rest.  Both are enqueued on the same
 // stream, so a captured graph holds them all.
 #define SPG_BATCH_DIRECT_ELEMS (1 << 22)
+#ifndef SPG_BATCH_S
 #define SPG_BATCH_S 4          // cp.async stages of the tiled path
+#endif
 #ifndef SPG_BATCH_MINB
-#define SPG_BATCH_MINB 1       // CTAs per SM the register allocation must allow
+#define SPG_BATCH_MINB 4       // CTAs per SM the register allocation must allow
 #endif
 
 struct BatchJob {
