@@ -37,7 +37,7 @@
 // stream, so a captured graph holds them all.
 #define SPG_BATCH_DIRECT_ELEMS (1 << 22)
 #ifndef SPG_BATCH_S
-#define SPG_BATCH_S 4          // cp.async stages of the tiled path
+#define SPG_BATCH_S 3          // cp.async stages of the tiled path
 #endif
 #ifndef SPG_BATCH_MINB
 #define SPG_BATCH_MINB 4       // CTAs per SM the register allocation must allow
