@@ -152,17 +152,19 @@ std::string plan_key(int rank, const int *dims, const int *perm, int op, int sms
 }
 
 int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
-                       bool allow_tma, Plan *pl);
+                       bool allow_tma, bool host_link, Plan *pl);
 int tma_smem_bytes(const TmaLayout &tl, int stages);
 
-// allow_tma: both tensors 16-byte aligned (the bulk tensor copies' rule)
+// allow_tma: both tensors 16-byte aligned device memory (the bulk tensor
+// copies' rule); host_link: a tensor is pinned host memory that the kernel
+// reads or writes in place over the host link
 int make_plan(int rank, const int *dims, const int *perm, double f, double g, int sms, Plan *pl,
-              bool allow_tma = true) {
+              bool allow_tma = true, bool host_link = false) {
     autoload_tune_file();
     if (rank < 1 || rank > SPG_MAXR || !dims || !perm)
-        return make_plan_uncached(rank, dims, perm, f, g, sms, allow_tma, pl);
+        return make_plan_uncached(rank, dims, perm, f, g, sms, allow_tma, host_link, pl);
     const int op = spg_choose_op(f, g);
-    const std::string key = plan_key(rank, dims, perm, op, sms) + (allow_tma ? "t" : "n");
+    const std::string key = plan_key(rank, dims, perm, op, sms) + (allow_tma ? "t" : "n") + (host_link ? "h" : "");
     {
         std::lock_guard<std::mutex> lk(g_plans_mu);
         auto it = g_plans.find(key);
@@ -172,7 +174,7 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
             return SPAGHETTY_OK;
         }
     }
-    int rc = make_plan_uncached(rank, dims, perm, f, g, sms, allow_tma, pl);
+    int rc = make_plan_uncached(rank, dims, perm, f, g, sms, allow_tma, host_link, pl);
     if (rc == SPAGHETTY_OK) {
         std::lock_guard<std::mutex> lk(g_plans_mu);
         if (g_plans.size() > 8192) g_plans.clear();
@@ -197,11 +199,31 @@ int to_tma(Plan *pl, int threads, int ept, int stages, bool strict) {
 }
 
 int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
-                       bool allow_tma, Plan *pl) {
+                       bool allow_tma, bool host_link, Plan *pl) {
     Folded fo;
     int rc = spg_fold(rank, dims, perm, &fo);
     if (rc) return rc;
     const int op = spg_choose_op(f, g);
+    if (host_link && !fo.empty && fo.rank >= 2) {
+        // over the host link long output rows matter most (measured on
+        // GB300, pinned buffers at 100^4: up to 15% over the device plan):
+        // the greedy box with 32-double input and 128-double output rows
+        // grown towards 4096 elements on the cp.async kernel (the smallest
+        // of 128/256/512 threads x 8 that holds it), 3 stages; the
+        // device-memory tune table does not apply
+        int box[SPG_MAXR];
+        Plan tp;
+        if (spg_box_greedy(fo, 32, 128, 4096, 4096, box) == SPAGHETTY_OK) {
+            int vol = 1;
+            for (int d = 0; d < fo.rank; ++d) vol *= box[d];
+            const int nt = vol <= 1024 ? 128 : (vol <= 2048 ? 256 : 512);
+            if (spg_plan(fo, op, box, nt, 8, 3, sms, &tp) == SPAGHETTY_OK &&
+                spg_build_params(&tp, f, g) == SPAGHETTY_OK && tp.kind == KIND_TILED) {
+                *pl = tp;
+                return SPAGHETTY_OK;
+            }
+        }
+    }
     TuneOverride ov;
     bool have = false;
     if (!fo.empty && fo.rank >= 2) {
@@ -595,7 +617,7 @@ int sort_sync(int rank, const double *u, double *s, const int *dims, const int *
     // tensor copies are not used
     const bool allow_tma = ku != 2 && ks != 2 && (ku == 1 ? aligned16(u) : true) &&
                            (ks == 1 ? aligned16(s) : true);
-    rc = make_plan(rank, dims, perm, f, g, device_sms(dev), &pl, allow_tma);
+    rc = make_plan(rank, dims, perm, f, g, device_sms(dev), &pl, allow_tma, ku == 2 || ks == 2);
     if (rc) return rc;
     cudaStream_t st = 0;  // legacy default stream: ordered after prior blocking-stream work
     const size_t n = (size_t)fo.nelem;
