@@ -231,7 +231,8 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         auto it = g_tune.find(tune_key(fo, op));
         if (it != g_tune.end()) { ov = it->second; have = true; }
     }
-    // an override with stages 12..14 asks for the TMA kernel (2..4 stages);
+    // an override with stages 12/13/14/16 asks for the TMA kernel (2/3/4/6
+    // load stages);
     // it is ignored where the TMA kernel cannot run (misaligned or host
     // buffers), which then get the default plan
     if (have && ov.stages >= 12 && !allow_tma) have = false;

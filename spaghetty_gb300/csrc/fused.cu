@@ -12,14 +12,17 @@
 // + ..., each product and each sum rounded exactly as the sequential calls
 // round them, so the result is bit-identical.
 //
-// Kernel: a persistent CTA walks boxes of the OUTPUT index space (box lengths
-// divide the extents, so no element masks).  For each box it loads its t3
-// elements into registers (output order), then for every source in turn
-// stages that source's elements through shared memory -- loaded in the
-// source's own memory order (coalesced), placed at their output-order slot --
-// and adds them.  Sources are double-buffered with cp.async: source k+1 is in
-// flight while source k is added.  Each source's box walk (offset and slot of
-// every element) is a shared-memory table built once per CTA.
+// Two kernels.  spg_fused_tma (below, first choice): a warp-specialised
+// TMA pipeline over three-dim output boxes, every source tile loaded by one
+// bulk tensor copy.  spg_fused_sortacc (shapes the bulk copies cannot
+// take): a persistent CTA walks boxes of the OUTPUT index space (box
+// lengths divide the extents, so no element masks).  For each box it loads
+// its t3 elements into registers (output order), then for every source in
+// turn stages that source's elements through shared memory -- loaded in the
+// source's own memory order (coalesced), placed at their output-order slot
+// -- and adds them.  Sources are double-buffered with cp.async: source k+1
+// is in flight while source k is added.  Each source's box walk (offset and
+// slot of every element) is a shared-memory table built once per CTA.
 #include "../../include/spaghetty_gb300.h"
 #include "kernels.cuh"
 #include "plan.h"
