@@ -297,7 +297,6 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
 
     if (tid == load_tid) {
         // ---- loads: item i of box it goes to slot j % S, j = it*items + i ----
-        const uint64_t pol = spg_l2_evict_first();
         bool ok = true;
         int64_t j = 0;
         int it = 0;
@@ -312,7 +311,7 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
                 spg_ft_coords(p, i, t, c);
                 const uint32_t mb = full0 + 8u * (uint32_t)s;
                 spg_mbar_expect_tx(mb, i == 0 ? p.tx_out : p.tx_src);
-                spg_tma_load5_hint(base + (uint32_t)s * tb, &maps.m[i], c, mb, pol);
+                spg_tma_load5(base + (uint32_t)s * tb, &maps.m[i], c, mb);
             }
         }
         if (!ok && p.status) *(volatile int *)p.status = 1;
@@ -322,7 +321,6 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
         return;
     }
     if (tid == store_tid) {
-        const uint64_t pol = spg_l2_evict_first();
         bool ok = true;
         int it = 0;
         for (uint32_t t = blockIdx.x; t < p.ntiles; t += G, ++it) {
@@ -331,7 +329,7 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
             if (!ok) break;
             int32_t c[5];
             spg_ft_coords(p, 0, t, c);
-            spg_tma_store5_hint(&maps.m[0], c, base + out0 + (uint32_t)o * tb, pol);
+            spg_tma_store5(&maps.m[0], c, base + out0 + (uint32_t)o * tb);
             spg_bulk_commit();
             spg_bulk_wait_read<0>();
             spg_mbar_arrive(free0 + 8u * (uint32_t)o);

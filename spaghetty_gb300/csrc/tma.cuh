@@ -69,30 +69,6 @@ __device__ __forceinline__ void spg_tma_store5(const void *tmap, const int32_t *
         "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4])
         : "memory");
 }
-// L2 policy "evict first" for the bulk copies: every element is loaded once
-// and stored once, so the copies should not push other data out of L2
-// (the same choice as the streaming loads and stores of the other kernels).
-__device__ __forceinline__ uint64_t spg_l2_evict_first() {
-    uint64_t pol;
-    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(pol));
-    return pol;
-}
-__device__ __forceinline__ void spg_tma_load5_hint(uint32_t dst, const void *tmap, const int32_t *c,
-                                                   uint32_t mbar, uint64_t pol) {
-    asm volatile(
-        "cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.L2::cache_hint"
-        " [%0], [%1, {%2, %3, %4, %5, %6}], [%7], %8;\n" ::"r"(dst),
-        "l"(tmap), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "r"(mbar), "l"(pol)
-        : "memory");
-}
-__device__ __forceinline__ void spg_tma_store5_hint(const void *tmap, const int32_t *c, uint32_t src,
-                                                    uint64_t pol) {
-    asm volatile(
-        "cp.async.bulk.tensor.5d.global.shared::cta.tile.bulk_group.L2::cache_hint"
-        " [%0, {%2, %3, %4, %5, %6}], [%1], %7;\n" ::"l"(tmap),
-        "r"(src), "r"(c[0]), "r"(c[1]), "r"(c[2]), "r"(c[3]), "r"(c[4]), "l"(pol)
-        : "memory");
-}
 __device__ __forceinline__ void spg_bulk_commit() {
     asm volatile("cp.async.bulk.commit_group;\n" ::: "memory");
 }
@@ -169,27 +145,21 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
     const uint32_t G = gridDim.x;
     const uint32_t load_tid = NT, store_tid = NT + 32;
 
-    uint64_t pol = 0;                       // L2 evict-first (load and store threads)
     auto issue = [&](uint32_t t, int s) {
         int32_t ci[5], co[5];
         spg_tma_coords(p, tp, t, ci, co);
         const uint32_t mb = full0 + 8u * (uint32_t)s;
         spg_mbar_expect_tx(mb, (uint32_t)tp.tx_bytes);
-        spg_tma_load5_hint(base + (uint32_t)s * sb, &tmap_in, ci, mb, pol);
-        if (spg_reads_out<OP>::value)
-            spg_tma_load5_hint(base + (uint32_t)s * sb + in_bytes, &tmap_out, co, mb, pol);
+        spg_tma_load5(base + (uint32_t)s * sb, &tmap_in, ci, mb);
+        if (spg_reads_out<OP>::value) spg_tma_load5(base + (uint32_t)s * sb + in_bytes, &tmap_out, co, mb);
         (void)co;
     };
     // the load thread sets up the barriers and fills every stage before the
     // permute threads build their tables, so DRAM latency overlaps the
     // prologue
     int issued = 0;                         // load thread: boxes whose loads were issued
-    if (tid == store_tid) {
-        spg_prefetch_tmap(&tmap_out);
-        pol = spg_l2_evict_first();
-    }
+    if (tid == store_tid) spg_prefetch_tmap(&tmap_out);
     if (tid == load_tid) {
-        pol = spg_l2_evict_first();
         spg_prefetch_tmap(&tmap_in);
         if (spg_reads_out<OP>::value) spg_prefetch_tmap(&tmap_out);
 #pragma unroll
@@ -252,7 +222,7 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
             if (!ok) break;
             int32_t ci[5], co[5];
             spg_tma_coords(p, tp, t, ci, co);
-            spg_tma_store5_hint(&tmap_out, co, base + out0 + (uint32_t)o * ob, pol);
+            spg_tma_store5(&tmap_out, co, base + out0 + (uint32_t)o * ob);
             spg_bulk_commit();
             // slot o is free again once this store has read it
             spg_bulk_wait_read<0>();
