@@ -352,6 +352,9 @@ int *status_word_dev() {
     return g_status_dev;
 }
 
+// L2 promotion of the bulk copies' requests: 128-byte measured 0.5% faster
+// on the sweep than 256-byte (TMA sorts at 100^4: 5875-5890 vs 5810 GB/s).
+#define SPG_L2_PROMOTION CU_TENSOR_MAP_L2_PROMOTION_L2_128B
 int encode_map(CUtensorMap *m, const double *ptr, const uint64_t *dim, const uint64_t *stride,
                const uint32_t *box, bool swizzle128 = false) {
     EncodeTiledFn fn = encode_fn();
@@ -363,7 +366,7 @@ int encode_map(CUtensorMap *m, const double *ptr, const uint64_t *dim, const uin
     CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 5, (void *)ptr, gd, gs, bd, es,
                     CU_TENSOR_MAP_INTERLEAVE_NONE,
                     swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
-                    CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                    SPG_L2_PROMOTION, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) {
         g_last_cuda.store(-(int)r);
         return SPAGHETTY_ERR_CUDA;
