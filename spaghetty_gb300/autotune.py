@@ -143,14 +143,26 @@ def candidates(dims: Sequence[int], perm: Sequence[int], op: int = 0):
             stages = (0,) if (p["kind"] == "direct" or ept < 2) else (0, 2, 3)
             for st in stages:
                 out.append((list(b), nt, ept, st))
-        # TMA-staged kernel (stages 12/13/14/16 = 2/3/4/6 load stages); the
-        # library rejects boxes that do not fit the bulk tensor copy rules
+        # TMA-staged kernel (stages 12/13/14/16 = 2/3/4/6 load stages) on the
+        # box with odd partial lengths along both stride-1 dims rounded up to
+        # even (the bulk copies move whole 16-byte units there); the library
+        # rejects boxes that do not fit the bulk tensor copy rules
+        bt = list(b)
+        for d in {len(D) - 1, P[len(D) - 1]}:
+            if bt[d] % 2 and bt[d] < D[d]:
+                bt[d] += 1
+        vol_t = 1
+        for x in bt:
+            vol_t *= x
+        if vol_t > VMAX:
+            continue
         for nt, ept in itertools.product(TMA_THREADS, TMA_EPTS):
             cap = nt * ept
-            if cap < vol or cap >= 2 * vol + nt:
+            if cap < vol_t or cap >= 2 * vol_t + nt:
                 continue
             for st in (12, 13, 14, 16):
-                out.append((list(b), nt, ept, st))
+                if (bt, nt, ept, st) not in out:
+                    out.append((bt, nt, ept, st))
     return p, out
 
 
@@ -302,6 +314,22 @@ def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False, dump=
     if not results:
         return None
     results.sort(key=lambda r: r[0])
+    # confirm: the four fastest and the default again, interleaved, with
+    # more repetitions, so that one noisy timing does not pick the winner
+    finalists = [cfg for _, cfg in results[:4]] + [None]
+    conf = {i: [] for i in range(len(finalists))}
+    for _ in range(3):
+        for i, cfg in enumerate(finalists):
+            clear()
+            if cfg is not None and _set(dims, perm, op, cfg) != 0:
+                continue
+            conf[i].append(time_case(dims, perm, op, reps, bufs=bufs))
+    clear()
+    med = {i: sorted(v)[len(v) // 2] for i, v in conf.items() if v}
+    t_default = med.get(len(finalists) - 1, t_default)
+    best_i = min((i for i in med if finalists[i] is not None), key=lambda i: med[i], default=None)
+    if best_i is not None:
+        results[0] = (med[best_i], finalists[best_i])
     t, (box, nt, ept, st) = results[0]
     if t_default < t:
         # the planner's own default beat every candidate: record it

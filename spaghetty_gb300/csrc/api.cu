@@ -267,6 +267,10 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         Plan tp;
         bool done = false;
         if (spg_box_greedy(fo, 32, 32, 4096, 4096, box) == SPAGHETTY_OK) {
+            // the bulk copies move whole 16-byte units along both stride-1
+            // dims: round an odd partial box length there up to even
+            for (const int d : {fo.rank - 1, fo.P[fo.rank - 1]})
+                if (box[d] % 2 && box[d] < fo.D[d]) box[d] += 1;
             int vol = 1;
             for (int d = 0; d < fo.rank; ++d) vol *= box[d];
             const int nt = vol <= 1024 ? 128 : 256, ept = vol <= 2048 ? 8 : 16;
