@@ -63,6 +63,10 @@ struct TuneOverride {
     int threads, ept, stages;
 };
 std::map<std::string, TuneOverride> g_tune;
+
+// Plain sorts on tuned TMA plans from this many elements (256 MiB per
+// array, twice GB300's L2) run on the power-of-two path (make_plan_uncached).
+#define SPG_TUNED_ONE_AS_POW2 (int64_t(1) << 25)
 std::map<int, int> g_sms;
 std::map<std::pair<const void *, int>, int> g_occ;
 
@@ -243,7 +247,20 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         if (rc) return rc;
         rc = spg_build_params(pl, f, g);
         if (rc) return rc;
-        if (want_tma) return to_tma(pl, ov.threads, ov.ept, ov.stages - 10, true);
+        if (want_tma) {
+            // The tuner times sorts with f = 0.5, so a plain sort (f = 1) of
+            // a large array on a tuned TMA plan runs that same kernel, as
+            // f = 2^0 on the power-of-two path (the same bits for every
+            // input but NaN, whose payload is not part of the contract).
+            // Measured on GB300: the bare shared-memory copy is 15-20%
+            // slower on the plans tuned at 100^4 (f = 1 sorts 5729 -> 6222
+            // GB/s on the sweep), but 2-4% faster on those tuned at 30^4
+            // and 50^4, whose arrays fit twice in L2; on untuned default
+            // plans neither is faster overall (0.93-1.08 across 50^4..100^4
+            // and 12^6..20^6).
+            if (pl->op == OP_SORT_ONE && fo.nelem >= SPG_TUNED_ONE_AS_POW2) pl->op = OP_SORT_POW2;
+            return to_tma(pl, ov.threads, ov.ept, ov.stages - 10, true);
+        }
         return SPAGHETTY_OK;
     }
     rc = spg_plan(fo, op, nullptr, 0, 0, 0, sms, pl);

@@ -29,33 +29,49 @@ static __device__ __noinline__ double spg_dmul_branch(double x, double f) {
     return __dmul_rn(x, f);
 }
 
-// x * f for f = +-2^k: when x is normal and x*f is normal, the product is
-// exact and equals x with k added to its exponent field and f's sign applied.
-// Exponent and sign live in the high 32-bit word, so this is 32-bit integer
-// work only (64-bit integer arithmetic on the bit pattern occupies GB300's
-// scarce FP64 pipe).  Every other input (zero, subnormal, inf, NaN) or
-// result (overflow, underflow) takes the rounded multiply, behind a warp
-// vote so that it is a real branch, so the bits always equal __dmul_rn(x, f).
-__device__ __forceinline__ double spg_pow2(double x, const SpgFactor &F) {
+// x * f for f = +-2^k on the integer path: when x and x*f are both normal
+// (the high word of x, sign bit cleared, in the window [elo, elo + erange)
+// that the host derives from k), the product is exact and equals x with k
+// added to its exponent field and f's sign applied; for x = +-0 only the
+// sign changes.  Exponent and sign live in the high 32-bit word, so this is
+// 32-bit integer work only (64-bit integer arithmetic on the bit pattern
+// occupies GB300's scarce FP64 pipe).  `exact` is cleared for every other
+// input (subnormal, inf, NaN) or result (overflow, underflow): those need the
+// rounded multiply.
+__device__ __forceinline__ double spg_pow2_fast(double x, const SpgFactor &F, bool &exact) {
     const uint32_t hi = (uint32_t)__double2hiint(x);
     const int lo = __double2loint(x);
-    const uint32_t e = (hi >> 20) & 0x7FFu;
-    const bool exact = e - 1u < 2046u && (uint32_t)((int32_t)e + F.k) - 1u < 2046u;
-    double r = __hiloint2double((int)((hi + ((uint32_t)F.k << 20)) ^ F.sgn_hi), lo);
+    const uint32_t h = hi & 0x7FFFFFFFu;
+    const bool inr = h - F.elo < F.erange;
+    exact = exact && (inr || (h | (uint32_t)lo) == 0u);
+    return __hiloint2double((int)((hi + (inr ? ((uint32_t)F.k << 20) : 0u)) ^ F.sgn_hi), lo);
+}
+
+// x * -1: the sign bit flipped (exact for every non-NaN x, inf included);
+// `exact` is cleared for NaN, which takes the multiply.
+__device__ __forceinline__ double spg_neg_fast(double x, bool &exact) {
+    const uint32_t hi = (uint32_t)__double2hiint(x);
+    const int lo = __double2loint(x);
+    const uint32_t mag = hi & 0x7FFFFFFFu;
+    exact = exact && (mag < 0x7FF00000u || (mag == 0x7FF00000u && lo == 0));
+    return __hiloint2double((int)(hi ^ 0x80000000u), lo);
+}
+
+// Per-element forms: the rare inexact cases take the rounded multiply behind
+// a warp vote, so that it is a real branch and the bits always equal
+// __dmul_rn(x, f).
+__device__ __forceinline__ double spg_pow2(double x, const SpgFactor &F) {
+    bool exact = true;
+    double r = spg_pow2_fast(x, F, exact);
     if (__any_sync(__activemask(), !exact)) {
         if (!exact) r = spg_dmul_branch(x, F.f);
     }
     return r;
 }
 
-// x * -1: the sign bit flipped (exact for every non-NaN x, inf included);
-// NaN takes the multiply.
 __device__ __forceinline__ double spg_neg(double x, const SpgFactor &F) {
-    const uint32_t hi = (uint32_t)__double2hiint(x);
-    const int lo = __double2loint(x);
-    const uint32_t mag = hi & 0x7FFFFFFFu;
-    const bool exact = mag < 0x7FF00000u || (mag == 0x7FF00000u && lo == 0);
-    double r = __hiloint2double((int)(hi ^ 0x80000000u), lo);
+    bool exact = true;
+    double r = spg_neg_fast(x, exact);
     if (__any_sync(__activemask(), !exact)) {
         if (!exact) r = spg_dmul_branch(x, F.f);
     }
@@ -77,6 +93,36 @@ __device__ __forceinline__ double spg_apply(double x, double y, const SpgFactor 
 
 template <int OP>
 struct spg_reads_out { static constexpr bool value = (OP >= OP_ACC_ONE); };
+
+// Two-phase form for the register-staged kernels, whose threads write EPT
+// elements of a box straight to global memory: spg_apply_fast gives every
+// element's integer-path result and clears `exact` where that is not the
+// rounded product; after one warp vote over all of them, a warp with any
+// such element recomputes its elements with spg_apply_mul, the rounded
+// arithmetic for every input.  No vote or branch sits between the elements,
+// so their shared-memory loads and global stores stay batched.  (The
+// TMA-staged kernel keeps the per-element form: there it measured faster.)
+template <int OP>
+struct spg_has_fast {
+    static constexpr bool value = OP == OP_SORT_NEG || OP == OP_SORT_POW2 ||
+                                  OP == OP_ACC_NEG || OP == OP_ACC_POW2;
+};
+
+template <int OP>
+__device__ __forceinline__ double spg_apply_fast(double x, double y, const SpgFactor &F, bool &exact) {
+    if (OP == OP_SORT_NEG) return spg_neg_fast(x, exact);
+    if (OP == OP_SORT_POW2) return spg_pow2_fast(x, F, exact);
+    if (OP == OP_ACC_NEG) return __dadd_rn(y, spg_neg_fast(x, exact));
+    if (OP == OP_ACC_POW2) return __dadd_rn(y, spg_pow2_fast(x, F, exact));
+    return spg_apply<OP>(x, y, F);
+}
+
+template <int OP>
+__device__ __forceinline__ double spg_apply_mul(double x, double y, const SpgFactor &F) {
+    if (OP == OP_SORT_NEG || OP == OP_SORT_POW2) return __dmul_rn(x, F.f);
+    if (OP == OP_ACC_NEG || OP == OP_ACC_POW2) return __dadd_rn(y, __dmul_rn(x, F.f));
+    return spg_apply<OP>(x, y, F);
+}
 
 // Every element is read once and written once: streaming (evict-first)
 // accesses.  Measured on GB300 (100^4, perm 4321): with default write-back
@@ -188,6 +234,44 @@ struct SpgTab {
     }
 };
 
+// Output phase of a register-staged box: this thread's element k goes from
+// staged-tile slot smr[k] to dst + ooff[k] (y[k]: the old output, sortacc).
+template <int NT, int EPT, int OP>
+__device__ __forceinline__ void spg_write_box(const SpgTab<NT, EPT> &tb, const double *tile,
+                                              const double (&y)[EPT], double *dst,
+                                              uint32_t limA, uint32_t limB, const SpgFactor &fac) {
+    if (spg_has_fast<OP>::value) {
+        double r[EPT];
+        bool exact = true;
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            r[k] = 0.0;
+            if (spg_valid(tb.pks[k], limA, limB))
+                r[k] = spg_apply_fast<OP>(tile[tb.smr[k]], spg_reads_out<OP>::value ? y[k] : 0.0,
+                                          fac, exact);
+        }
+        if (!__all_sync(__activemask(), exact)) {
+#pragma unroll
+            for (int k = 0; k < EPT; ++k)
+                if (spg_valid(tb.pks[k], limA, limB))
+                    r[k] = spg_apply_mul<OP>(tile[tb.smr[k]],
+                                             spg_reads_out<OP>::value ? y[k] : 0.0, fac);
+        }
+#pragma unroll
+        for (int k = 0; k < EPT; ++k)
+            if (spg_valid(tb.pks[k], limA, limB)) spg_st_out(dst + tb.ooff[k], r[k]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < EPT; ++k) {
+            if (spg_valid(tb.pks[k], limA, limB)) {
+                const double x = tile[tb.smr[k]];
+                spg_st_out(dst + tb.ooff[k],
+                           spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, fac));
+            }
+        }
+    }
+}
+
 // One box of the register-staged tiled kernel.  Contains two CTA barriers:
 // every thread of the CTA must call it for the same box.
 template <int NT, int EPT, int OP>
@@ -219,14 +303,7 @@ __device__ __forceinline__ void spg_tiled_box(const KParams &p, const SpgTab<NT,
             if (spg_valid(tb.pks[k], limA, limB)) y[k] = spg_ld_out(dst + tb.ooff[k]);
         }
     }
-#pragma unroll
-    for (int k = 0; k < EPT; ++k) {
-        if (spg_valid(tb.pks[k], limA, limB)) {
-            const double x = sm[tb.smr[k]];
-            spg_st_out(dst + tb.ooff[k],
-                       spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, fac));
-        }
-    }
+    spg_write_box<NT, EPT, OP>(tb, sm, y, dst, limA, limB, fac);
 }
 
 // One box of the direct kernel (no barrier).
@@ -338,14 +415,7 @@ spg_tiled_async(const double *__restrict__ in, double *__restrict__ out,
                 if (spg_valid(tb.pks[k], limA, limB)) y[k] = spg_ld_out(dst + tb.ooff[k]);
             }
         }
-#pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            if (spg_valid(tb.pks[k], limA, limB)) {
-                const double x = tile[tb.smr[k]];
-                spg_st_out(dst + tb.ooff[k],
-                           spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, fac));
-            }
-        }
+        spg_write_box<NT, EPT, OP>(tb, tile, y, dst, limA, limB, fac);
     }
     spg_cp_wait<0>();
 }

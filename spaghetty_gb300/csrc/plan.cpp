@@ -117,9 +117,18 @@ SpgFactor spg_make_factor(double f, double g) {
     F.f = f;
     F.g = g;
     int k = 0;
-    if (factor_class(f, &k) == 2) {
+    const int fc = factor_class(f, &k);
+    // f = 1 gets the fields of 2^0 too: the TMA-staged kernel runs plain
+    // sorts on the power-of-two path
+    if (fc == 0 || fc == 2) {
         F.k = k;
         F.sgn_hi = std::signbit(f) ? 0x80000000u : 0u;
+        // biased exponents e of x with 1 <= e <= 2046 and 1 <= e + k <= 2046
+        const int elo = std::max(1, 1 - k), ehi = std::min(2046, 2046 - k);
+        if (elo <= ehi) {
+            F.elo = (uint32_t)elo << 20;
+            F.erange = (uint32_t)(ehi - elo + 1) << 20;
+        }
     }
     return F;
 }

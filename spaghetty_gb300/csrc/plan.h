@@ -63,6 +63,9 @@ struct SpgFactor {
     double f, g;
     int32_t k;          // f = +-2^k
     uint32_t sgn_hi;    // sign bit of f in the high 32-bit word
+    // high words (sign bit cleared) of the x for which x and x*2^k are both
+    // normal: elo <= hi(x) & 0x7FFFFFFF < elo + erange (erange 0: none)
+    uint32_t elo, erange;
 };
 
 struct KParams {

@@ -59,3 +59,86 @@ def test_factor_class_bits(cuda, f, acc):
             with np.errstate(all="ignore"):
                 wnt = O.np_sort(x, dims, perm, f, 1.0 if acc else 0.0, out=y)
         assert same_bits(got, wnt), (f, acc, perm, first_mismatch(got, wnt))
+
+
+@pytest.mark.parametrize("density", ["dense", "sparse"])
+def test_factor_class_bits_tma(cuda, density):
+    """The same bits through forced TMA-staged plans, whose permute threads
+    take the integer path and fall back to the rounded multiply behind a
+    warp vote: edge values everywhere (most votes take the multiply) or
+    sprinkled among ordinary values (a few do), zeros on the integer path.
+    Plain sorts (f = 1) on a tuned TMA plan run that path as f = 2^0."""
+    from spaghetty_gb300._lib import int_array, lib
+    from spaghetty_gb300.autotune import candidates, clear
+    dims = (8, 12, 10, 16)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(17)
+    edges = edge_values()
+    if density == "dense":
+        x = np.resize(edges, n)
+        y = np.resize(np.flip(edge_values(seed=9)), n)
+    else:
+        x = rng.uniform(-2, 2, n)
+        y = rng.uniform(-2, 2, n)
+        pos = rng.choice(n, 40, replace=False)
+        x[pos] = rng.choice(edges[:28], 40)
+        y[pos[:10]] = rng.choice(edges[:28], 10)
+    L = lib()
+    ran = 0
+    try:
+        for perm in [(4, 3, 2, 1), (2, 3, 4, 1), (1, 3, 4, 2)]:
+            for f in (1.0, -1.0, 0.5, -(2.0 ** 600), 2.0 ** -1030, 2.0 ** 1000):
+                for acc in (False, True):
+                    g = 1.0 if acc else 0.0
+                    with np.errstate(all="ignore"):
+                        want = O.np_sort(x, dims, perm, f, g, out=y)
+                    _, cands = candidates(dims, perm, int(acc))
+                    tma = [c for c in cands if c[3] >= 12][:2]
+                    for box, nt, ept, st in tma:
+                        if L.spaghetty_tune_set(4, int_array(dims), int_array(perm), int(acc),
+                                                int_array(box), nt, ept, st) != 0:
+                            continue
+                        du = torch.from_numpy(x).to(cuda)
+                        ds = torch.from_numpy(y.copy()).to(cuda)
+                        sort_generic(du, ds, dims, perm, f, g)
+                        got = ds.cpu().numpy()
+                        assert same_bits(got, want), (f, acc, perm, box, nt, ept, st,
+                                                      first_mismatch(got, want))
+                        ran += 1
+                clear()
+    finally:
+        clear()
+    assert ran > 0
+
+
+def test_plain_sort_large_tuned_tma_bits(cuda):
+    """A plain sort (f = 1) of 2^25 elements on a tuned TMA plan, which runs
+    the power-of-two path as f = 2^0: the input's bits, edge values
+    included."""
+    from spaghetty_gb300._lib import int_array, lib
+    from spaghetty_gb300.autotune import candidates, clear
+    dims = (32, 32, 128, 256)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(23)
+    x = rng.uniform(-2, 2, n)
+    pos = rng.choice(n, 2000, replace=False)
+    x[pos] = rng.choice(edge_values()[:28], 2000)
+    L = lib()
+    ran = 0
+    try:
+        for perm in [(4, 3, 2, 1), (2, 1, 4, 3)]:
+            want = O.np_sort(x, dims, perm, 1.0, 0.0)
+            _, cands = candidates(dims, perm, 0)
+            box, nt, ept, st = [c for c in cands if c[3] >= 12][0]
+            assert L.spaghetty_tune_set(4, int_array(dims), int_array(perm), 0,
+                                        int_array(box), nt, ept, st) == 0
+            du = torch.from_numpy(x).to(cuda)
+            ds = torch.empty_like(du)
+            sort_generic(du, ds, dims, perm, 1.0, 0.0)
+            got = ds.cpu().numpy()
+            assert same_bits(got, want), (perm, first_mismatch(got, want))
+            ran += 1
+            clear()
+    finally:
+        clear()
+    assert ran == 2
