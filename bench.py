@@ -277,7 +277,7 @@ def run_ours(args, ws, rank, local):
         del bufs
         torch.cuda.empty_cache()
         secondary = {"sort6": run_sort6(args, dev), "triples_fused": run_fused(args, dev),
-                     "autograd": run_autograd(args, dev)}
+                     "autograd": run_autograd(args, dev), "contract": run_contract(args, dev)}
         torch.cuda.empty_cache()
     batched = None
     if not args.no_batched:
@@ -662,6 +662,53 @@ def run_autograd(args, dev):
         t = _timed_events(step, 10, stream)
         res["x".join(map(str, dims))] = {"fwd_bwd_gbs": round(2 * (16 + 2 * 24) * n / t / 1e9, 1),
                                           "ms": round(t * 1e3, 4)}
+    return res
+
+
+def run_contract(args, dev):
+    """The macaroni skeleton's CCSD term (ccsd_t2_8: sort 4321, sort 2143,
+    dgemm('T','N'), sort 2143) at d^6 index extents: the fused kernel in its
+    exact mode (loop_dgemm's bits) and fma mode, against the same chain
+    unfused -- three sort launches around cuBLAS's DGEMM (torch.matmul).
+    FP64-bound; operands are L2-resident at these sizes, nothing is flushed.
+    GFLOP/s counts 2*M*N*K."""
+    import torch
+    import spaghetty_gb300 as S
+    from spaghetty_gb300.contract import contract_4x4
+    stream = torch.cuda.current_stream(dev)
+    res = {}
+    for d in (16, 24):
+        d1 = d2 = d3 = d4 = d5 = d6 = d
+        M, N, K = d1 * d2, d3 * d4, d5 * d6
+        t = torch.rand(d5 * d6 * d1 * d2, dtype=torch.float64, device=dev) - 0.5
+        v = torch.rand(d3 * d4 * d5 * d6, dtype=torch.float64, device=dev) - 0.5
+        c = torch.empty(d1 * d2 * d3 * d4, dtype=torch.float64, device=dev)
+        a_s = torch.empty_like(t)
+        b_s = torch.empty_like(v)
+        c_s = torch.empty_like(c)
+        da, db = (d5, d6, d1, d2), (d3, d4, d5, d6)
+
+        def fused(mode):
+            contract_4x4(t, da, (4, 3, 2, 1), v, db, (2, 1, 4, 3), c, (2, 1, 4, 3), mode=mode)
+
+        def unfused():
+            S.sort_generic(t, a_s, da, (4, 3, 2, 1), 1.0, 0.0)
+            S.sort_generic(v, b_s, db, (2, 1, 4, 3), 1.0, 0.0)
+            # c_sort (column-major M x N) = a_sort^T b_sort, i.e. C-order [N][M]
+            torch.matmul(b_s.view(N, K), a_s.view(M, K).t(), out=c_s.view(N, M))
+            S.sort_generic(c_s, c, (d4, d3, d2, d1), (2, 1, 4, 3), 1.0, 0.0)
+
+        row = {}
+        for name, fn in (("fused_exact", lambda: fused("exact")), ("fused_fma", lambda: fused("fma")),
+                         ("unfused_cublas", unfused)):
+            for _ in range(3):
+                fn()
+            tm = _timed_events(fn, 10, stream)
+            row[name] = {"ms": round(tm * 1e3, 4), "gflops": round(2.0 * M * N * K / tm / 1e9, 1)}
+        row["fma_vs_unfused"] = round(row["unfused_cublas"]["ms"] / row["fused_fma"]["ms"], 2)
+        row["exact_vs_unfused"] = round(row["unfused_cublas"]["ms"] / row["fused_exact"]["ms"], 2)
+        res["%d^6" % d] = row
+        del t, v, c, a_s, b_s, c_s
     return res
 
 

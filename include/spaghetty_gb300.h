@@ -380,6 +380,52 @@ int spaghetty_batch_destroy(spaghetty_batch *batch);
  * Returns a SPAGHETTY_* code. */
 int spaghetty_batch_tune_set(int rank, int ext_lo, int ext_hi, int run_in, int run_out, int volume);
 
+/* ---- a contraction with its sorts fused --------------------------------- */
+
+/* The TCE pattern sort -> DGEMM('T','N') -> sort in one kernel
+ * (branches/old/python/macaroni/ccsd_t2_8_skeleton.F:174-184), rank-4
+ * operands with two contracted indices.  With a_sort = a.permute(perm_a-1)
+ * of dims (SA0,SA1,SA2,SA3) read as the matrix [M=SA0*SA1][K=SA2*SA3], and
+ * b_sort = b.permute(perm_b-1) of dims (SB0,SB1,SA2,SA3) as [N][K]:
+ *   c_sort[n][m] = Sum_k (alpha*a_sort[m][k]) * b_sort[n][k],  dims (SB0,SB1,SA0,SA1)
+ *   c = factor * c_sort.permute(perm_c-1)             (acc_factor 0), or
+ *   c = c + factor * c_sort.permute(perm_c-1)         (acc_factor 1), or
+ *   c = acc_factor*c + factor*(...)                   (otherwise),
+ * as tce_sort_4 / tce_sortacc_4 of c_sort round them.  mode 0: k ascending,
+ * every product and sum rounded -- the bits of the skeleton's loop_dgemm
+ * case 3 (ccsd_t2_8_skeleton.F:214-292) on a zeroed c_sort; mode 1: the
+ * same order with fused multiply-adds (faster, not bit-identical).  Dims
+ * and perms are 4 ints each (1-based perms); the operands must agree on the
+ * contracted dims (else SPAGHETTY_ERR_DIMS).  Device (or managed) memory of
+ * one device, else SPAGHETTY_ERR_MEMSPACE; asynchronous on `stream`. */
+int spaghetty_contract_4x4(const double *a, const int *dims_a, const int *perm_a,
+                           const double *b, const int *dims_b, const int *perm_b,
+                           double *c, const int *perm_c, double alpha, double factor,
+                           double acc_factor, int mode, void *stream);
+
+/* The last SPAGHETTY_* code of the contraction entries on this thread. */
+int spaghetty_contract_last_error(void);
+
+/* The macaroni skeleton's subroutine, drop-in
+ * (ccsd_t2_8_skeleton.F:174-184): i0(p3,p4,h1,h2) = Sum(p5,p6)
+ * v(p3,p4,p5,p6) * t(p5,p6,h1,h2) with a_raw = t of dims (dim5,dim6,dim1,
+ * dim2), b_raw = v of dims (dim3,dim4,dim5,dim6) and c_done of dims
+ * (dim3,dim4,dim1,dim2), last index stride-1; c_done is overwritten.  The
+ * sizes must hold those element counts.  Host or device memory, synchronous;
+ * mode 0 arithmetic (bit-identical to the skeleton's loop_dgemm path).  The
+ * void forms print 'something is wrong...' and a line naming the problem on
+ * a bad argument; the _status form returns the code. */
+void ccsd_t2_8(const double *a_raw, const int *size_a, const double *b_raw, const int *size_b,
+               double *c_done, const int *size_c, const int *dim1, const int *dim2,
+               const int *dim3, const int *dim4, const int *dim5, const int *dim6);
+void ccsd_t2_8_(const double *a_raw, const int *size_a, const double *b_raw, const int *size_b,
+                double *c_done, const int *size_c, const int *dim1, const int *dim2,
+                const int *dim3, const int *dim4, const int *dim5, const int *dim6);
+int ccsd_t2_8_status(const double *a_raw, const int *size_a, const double *b_raw,
+                     const int *size_b, double *c_done, const int *size_c, const int *dim1,
+                     const int *dim2, const int *dim3, const int *dim4, const int *dim5,
+                     const int *dim6);
+
 /* Batched sorts for callers that cannot allocate device memory -- code
  * running while a CUDA graph is being captured (where cudaMalloc is not
  * allowed), or inside an application that owns the whole device memory

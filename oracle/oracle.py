@@ -29,17 +29,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "liboracle.so")
 SRC_PATH = os.path.join(HERE, "old_sort.c")
+SRC_PATHS = [SRC_PATH, os.path.join(HERE, "loop_dgemm.c")]
 
 _lib = None
 
 
 def build(force: bool = False) -> str:
-    """Compile old_sort.c into liboracle.so (gcc, no FMA contraction)."""
+    """Compile old_sort.c and loop_dgemm.c into liboracle.so (gcc, no FMA
+    contraction)."""
     if force or not os.path.exists(LIB_PATH) or (
-            os.path.getmtime(LIB_PATH) < os.path.getmtime(SRC_PATH)):
+            os.path.getmtime(LIB_PATH) < max(os.path.getmtime(p) for p in SRC_PATHS)):
         tmp = LIB_PATH + ".tmp%d" % os.getpid()
         subprocess.check_call(["gcc", "-O2", "-std=c99", "-ffp-contract=off",
-                               "-fPIC", "-shared", SRC_PATH, "-o", tmp])
+                               "-fPIC", "-shared"] + SRC_PATHS + ["-o", tmp])
         os.replace(tmp, LIB_PATH)
     return LIB_PATH
 
@@ -63,6 +65,9 @@ def lib():
             fn = getattr(L, "oracle_old_sort%s_8" % acc)
             fn.argtypes = [dp, dp, ip, ip, dp]
             fn.restype = None
+        L.oracle_loop_dgemm.argtypes = [ctypes.c_double, ctypes.c_double, dp, dp, dp] + \
+            [ctypes.c_int] * 7
+        L.oracle_loop_dgemm.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -143,6 +148,48 @@ def np_sort(u: np.ndarray, dims: Sequence[int], perm: Sequence[int],
     if acc_factor == 1.0:
         return np.add(y, prod)
     return np.add(np.multiply(y, np.float64(acc_factor)), prod)
+
+
+def loop_dgemm(alpha: float, beta: float, a: np.ndarray, b: np.ndarray, c: np.ndarray,
+               row_a: int, col_a: int, row_b: int, col_b: int, row_c: int, col_c: int,
+               case: int) -> np.ndarray:
+    """The skeleton's reference DGEMM (loop_dgemm.c, restating
+    branches/old/python/macaroni/ccsd_t2_8_skeleton.F:214-292) on flat
+    column-major buffers; updates ``c`` in place and returns it."""
+    a = np.ascontiguousarray(a, dtype=np.float64).reshape(-1)
+    b = np.ascontiguousarray(b, dtype=np.float64).reshape(-1)
+    flat = c.reshape(-1)
+    assert flat.dtype == np.float64 and flat.flags.c_contiguous
+    rc = lib().oracle_loop_dgemm(float(alpha), float(beta), _dptr(a), _dptr(b), _dptr(flat),
+                                 row_a, col_a, row_b, col_b, row_c, col_c, case)
+    if rc != 0:
+        raise ValueError("loop_dgemm: shapes do not match case %d" % case)
+    return c
+
+
+def contract_4x4(a: np.ndarray, dims_a: Sequence[int], perm_a: Sequence[int],
+                 b: np.ndarray, dims_b: Sequence[int], perm_b: Sequence[int],
+                 perm_c: Sequence[int], alpha: float = 1.0, factor: float = 1.0,
+                 acc_factor: float = 0.0, out: np.ndarray | None = None) -> np.ndarray:
+    """The skeleton's sort -> DGEMM('T','N') -> sort chain
+    (ccsd_t2_8_skeleton.F:174-184) with loop_dgemm case 3 as the DGEMM, on a
+    zeroed c_sort with beta = 1: a_sort = sort(a, perm_a) read as the
+    column-major K x M matrix, b_sort = sort(b, perm_b) as K x N, c_sort
+    (M x N column-major, i.e. C-order dims (SB0,SB1,SA0,SA1)) =
+    Sum_k (alpha*a)*b, then the result sort (factor, acc_factor) into
+    ``out``.  Returns the flat result."""
+    sa = [int(dims_a[p - 1]) for p in perm_a]
+    sb = [int(dims_b[p - 1]) for p in perm_b]
+    assert sa[2:] == sb[2:], "contracted dims differ"
+    M, N, K = sa[0] * sa[1], sb[0] * sb[1], sa[2] * sa[3]
+    a_sort = sort_generic(a, dims_a, perm_a, 1.0, 0.0)
+    b_sort = sort_generic(b, dims_b, perm_b, 1.0, 0.0)
+    c_sort = np.zeros(M * N)
+    loop_dgemm(alpha, 1.0, a_sort, b_sort, c_sort, K, M, K, N, M, N, 3)
+    cs = (sb[0], sb[1], sa[0], sa[1])
+    if out is None:
+        out = np.zeros(M * N)
+    return sort_generic(c_sort, cs, perm_c, factor, acc_factor, out)
 
 
 def init_array(dims: Sequence[int]) -> np.ndarray:

@@ -59,6 +59,8 @@ _R4 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 8 + [c_double_p]
 _R6 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 12 + [c_double_p]
 _R8 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 16 + [c_double_p]
 _R2 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int_p] * 4 + [c_double_p]
+# ccsd_t2_8(a_raw, size_a, b_raw, size_b, c_done, size_c, dim1..dim6)
+_T2_8 = [ctypes.c_void_p, c_int_p, ctypes.c_void_p, c_int_p, ctypes.c_void_p, c_int_p] + [c_int_p] * 6
 
 c_int64_p = ctypes.POINTER(ctypes.c_int64)
 _R4_I8 = [ctypes.c_void_p, ctypes.c_void_p] + [c_int64_p] * 8 + [c_double_p]
@@ -113,6 +115,13 @@ PROTOTYPES = {
                                                ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
                                                ctypes.c_void_p]),
     "spaghetty_sort_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "spaghetty_contract_4x4": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, ctypes.c_void_p,
+                                              c_int_p, c_int_p, ctypes.c_void_p, c_int_p,
+                                              ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                                              ctypes.c_int, ctypes.c_void_p]),
+    "spaghetty_contract_last_error": (ctypes.c_int, []),
+    "ccsd_t2_8": (None, _T2_8), "ccsd_t2_8_": (None, _T2_8),
+    "ccsd_t2_8_status": (ctypes.c_int, _T2_8),
     "spaghetty_selftest": (ctypes.c_int, []),
     "spaghetty_version": (ctypes.c_char_p, []),
 }

@@ -1,0 +1,87 @@
+"""The fused contraction's oracle on the CPU: loop_dgemm.c (the skeleton's
+reference DGEMM, branches/old/python/macaroni/ccsd_t2_8_skeleton.F:214-292)
+and the sort -> DGEMM -> sort chain (:174-184), pinned against numpy and,
+as the skeleton itself checks its dgemm, exactly on the number_array fill
+(:439-447) whose sums are all exact."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+
+def colmajor(flat, rows, cols):
+    return flat.reshape(cols, rows).T
+
+
+@pytest.mark.parametrize("case", [1, 2, 3, 4])
+def test_loop_dgemm_every_case_matches_numpy(case):
+    rng = np.random.default_rng(case)
+    m, n, k = 7, 5, 9
+    if case == 1:
+        ra, ca, rb, cb = m, k, k, n
+    elif case == 2:
+        ra, ca, rb, cb = m, k, n, k
+    elif case == 3:
+        ra, ca, rb, cb = k, m, k, n
+    else:
+        ra, ca, rb, cb = k, m, n, k
+    a = rng.uniform(-1, 1, ra * ca)
+    b = rng.uniform(-1, 1, rb * cb)
+    c0 = rng.uniform(-1, 1, m * n)
+    A, B = colmajor(a, ra, ca), colmajor(b, rb, cb)
+    opa = A if case in (1, 2) else A.T
+    opb = B if case in (1, 3) else B.T
+    want = 0.5 * colmajor(c0, m, n) - 1.5 * (opa @ opb)
+    c = c0.copy()
+    O.loop_dgemm(-1.5, 0.5, a, b, c, ra, ca, rb, cb, m, n, case)
+    np.testing.assert_allclose(colmajor(c, m, n), want, rtol=1e-13, atol=1e-13)
+
+
+def test_loop_dgemm_refuses_mismatched_shapes():
+    a = np.zeros(6)
+    with pytest.raises(ValueError):
+        O.loop_dgemm(1.0, 0.0, a, a, a.copy(), 2, 3, 2, 3, 2, 3, 3)
+
+
+def test_skeleton_number_array_fill_is_exact():
+    """ccsd_t2_8_skeleton.F:60-158: number_array operands, tce_sort_4 4321
+    and 2143, dgemm('T','N') checked against loop_dgemm case 3 with
+    compare_arrays (exact); the sums are integers below 2^53, so any
+    summation order gives these bits."""
+    d1, d2, d3, d4, d5, d6 = 8, 9, 4, 5, 6, 7
+    t = np.arange(1, d5 * d6 * d1 * d2 + 1, dtype=np.float64)
+    v = np.arange(1, d3 * d4 * d5 * d6 + 1, dtype=np.float64)
+    got = O.contract_4x4(t, (d5, d6, d1, d2), (4, 3, 2, 1), v, (d3, d4, d5, d6), (2, 1, 4, 3),
+                         (2, 1, 4, 3))
+    want = np.einsum("cdab,efcd->efab", t.reshape(d5, d6, d1, d2).astype(np.int64),
+                     v.reshape(d3, d4, d5, d6).astype(np.int64)).reshape(-1)
+    assert np.array_equal(got, want.astype(np.float64))
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_contract_chain_matches_einsum(seed):
+    """Random perms of both operands and of the result, every factor case."""
+    rng = np.random.default_rng(seed)
+    pa = tuple(int(x) + 1 for x in rng.permutation(4))
+    pb = tuple(int(x) + 1 for x in rng.permutation(4))
+    pc = tuple(int(x) + 1 for x in rng.permutation(4))
+    sa = list(rng.integers(2, 6, 4))
+    sb = list(rng.integers(2, 6, 2)) + sa[2:]
+    # raw dims whose permutation gives the sorted dims
+    da = [0] * 4
+    db = [0] * 4
+    for q in range(4):
+        da[pa[q] - 1] = int(sa[q])
+        db[pb[q] - 1] = int(sb[q])
+    a = rng.uniform(-1, 1, int(np.prod(da)))
+    b = rng.uniform(-1, 1, int(np.prod(db)))
+    a_s = a.reshape(da).transpose([p - 1 for p in pa]).reshape(sa[0] * sa[1], -1)
+    b_s = b.reshape(db).transpose([p - 1 for p in pb]).reshape(sb[0] * sb[1], -1)
+    c_sort = (b_s @ a_s.T).reshape(sb[0], sb[1], sa[0], sa[1])
+    c_ref = c_sort.transpose([p - 1 for p in pc]).reshape(-1)
+    for f, g in ((1.0, 0.0), (-0.5, 1.0), (0.3, 2.0)):
+        y = rng.uniform(-1, 1, c_ref.size)
+        got = O.contract_4x4(a, da, pa, b, db, pb, pc, alpha=0.75, factor=f, acc_factor=g,
+                             out=y.copy())
+        want = g * y + f * 0.75 * c_ref
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
