@@ -26,10 +26,10 @@
 // The result goes through the sorts' factor arithmetic: c_done = f*s (sort)
 // or c_done + f*s (sortacc), exactly as tce_sort_4 / tce_sortacc_4 of c_sort.
 //
-// GB300 has a narrow FP64 pipe (about 1.3 operations per SM per clock): the
-// kernel is bound by it, not by memory.  A 16x16 output tile per 64-thread
-// CTA keeps every SM busy even for the small tiles of CCSD (M = N = 256),
-// and each operand element, once in shared memory, serves 16 products.
+// GB300 has a narrow FP64 pipe (about 1.5 operations per SM per clock): the
+// kernel is bound by it, not by memory.  A 16x16 output tile per CTA keeps
+// every SM busy even for the small tiles of CCSD (M = N = 256), and each
+// operand element, once in shared memory, serves 16 products.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -46,7 +46,6 @@
 #define SPG_CT_TM 16   // output tile: m
 #define SPG_CT_TN 16   // output tile: n
 #define SPG_CT_TK 32   // contracted indices staged per step
-#define SPG_CT_NT 64   // 8 x 8 threads, 2 x 2 outputs each
 
 // Offset of a two-index group x = x0*e1 + x1 inside a raw tensor:
 // x0*w0 + x1*w1.
@@ -73,14 +72,18 @@ __device__ __forceinline__ int64_t spg_g2(const SpgGroup2 &g, uint32_t x) {
     return (int64_t)x0 * g.w0 + (int64_t)(x - x0 * g.e1v) * g.w1;
 }
 
-template <int OP, bool FMA>
-__global__ void __launch_bounds__(SPG_CT_NT)
+// RM x RN outputs per thread; (16/RM) x (16/RN) threads per CTA.
+template <int OP, bool FMA, int RM, int RN>
+__global__ void __launch_bounds__((SPG_CT_TM / RM) * (SPG_CT_TN / RN))
 spg_contract(const __grid_constant__ ContractParams p) {
+    constexpr int TMX = SPG_CT_TM / RM;             // threads along m
+    constexpr int NT = TMX * (SPG_CT_TN / RN);
+    constexpr int KROWS = NT / 16;                  // k rows one staging pass covers
     __shared__ __align__(16) double As[SPG_CT_TK][SPG_CT_TM];
     __shared__ __align__(16) double Bs[SPG_CT_TK][SPG_CT_TN];
     const uint32_t tid = threadIdx.x;
-    const uint32_t tx = tid & 7u, ty = tid >> 3;
-    // staging: this thread loads tile rows (tid & 15) at k rows (tid >> 4) + 4j
+    const uint32_t tx = tid % TMX, ty = tid / TMX;
+    // staging: this thread loads tile row (tid & 15) at k rows (tid >> 4) + KROWS*j
     const uint32_t lrow = tid & 15u, lk = tid >> 4;
     const SpgFactor fac = p.fac;
     for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
@@ -90,12 +93,16 @@ spg_contract(const __grid_constant__ ContractParams p) {
         const bool lm_ok = m0 + lrow < (uint32_t)p.M, ln_ok = n0 + lrow < (uint32_t)p.N;
         const int64_t offa = lm_ok ? spg_g2(p.am, m0 + lrow) : 0;
         const int64_t offb = ln_ok ? spg_g2(p.bn, n0 + lrow) : 0;
-        double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+        double acc[RM][RN];
+#pragma unroll
+        for (int i = 0; i < RM; ++i)
+#pragma unroll
+            for (int j = 0; j < RN; ++j) acc[i][j] = 0.0;
         for (int32_t k0 = 0; k0 < p.K; k0 += SPG_CT_TK) {
             __syncthreads();                // the previous step's tiles are consumed
 #pragma unroll
-            for (int j = 0; j < SPG_CT_TK / 4; ++j) {
-                const uint32_t kk = lk + 4u * j;
+            for (int j = 0; j < SPG_CT_TK / KROWS; ++j) {
+                const uint32_t kk = lk + (uint32_t)KROWS * j;
                 const uint32_t k = (uint32_t)k0 + kk;
                 double va = 0.0, vb = 0.0;
                 if (k < (uint32_t)p.K) {
@@ -112,30 +119,28 @@ spg_contract(const __grid_constant__ ContractParams p) {
             const int32_t kn = min(SPG_CT_TK, p.K - k0);
             // k strictly ascending: the loop's order of additions
             for (int32_t kk = 0; kk < kn; ++kk) {
-                const double2 a2 = *reinterpret_cast<const double2 *>(&As[kk][2 * tx]);
-                const double2 b2 = *reinterpret_cast<const double2 *>(&Bs[kk][2 * ty]);
-                if (FMA) {
-                    acc[0][0] = __fma_rn(a2.x, b2.x, acc[0][0]);
-                    acc[0][1] = __fma_rn(a2.x, b2.y, acc[0][1]);
-                    acc[1][0] = __fma_rn(a2.y, b2.x, acc[1][0]);
-                    acc[1][1] = __fma_rn(a2.y, b2.y, acc[1][1]);
-                } else {
-                    acc[0][0] = __dadd_rn(acc[0][0], __dmul_rn(a2.x, b2.x));
-                    acc[0][1] = __dadd_rn(acc[0][1], __dmul_rn(a2.x, b2.y));
-                    acc[1][0] = __dadd_rn(acc[1][0], __dmul_rn(a2.y, b2.x));
-                    acc[1][1] = __dadd_rn(acc[1][1], __dmul_rn(a2.y, b2.y));
-                }
+                double av[RM], bv[RN];
+#pragma unroll
+                for (int i = 0; i < RM; ++i) av[i] = As[kk][RM * tx + i];
+#pragma unroll
+                for (int j = 0; j < RN; ++j) bv[j] = Bs[kk][RN * ty + j];
+#pragma unroll
+                for (int i = 0; i < RM; ++i)
+#pragma unroll
+                    for (int j = 0; j < RN; ++j)
+                        acc[i][j] = FMA ? __fma_rn(av[i], bv[j], acc[i][j])
+                                        : __dadd_rn(acc[i][j], __dmul_rn(av[i], bv[j]));
             }
         }
         // each result element written once, at its sorted position
 #pragma unroll
-        for (int i = 0; i < 2; ++i) {
-            const uint32_t m = m0 + 2 * tx + i;
+        for (int i = 0; i < RM; ++i) {
+            const uint32_t m = m0 + RM * tx + i;
             if (m >= (uint32_t)p.M) continue;
             const int64_t ocm = spg_g2(p.cm, m);
 #pragma unroll
-            for (int j = 0; j < 2; ++j) {
-                const uint32_t n = n0 + 2 * ty + j;
+            for (int j = 0; j < RN; ++j) {
+                const uint32_t n = n0 + RN * ty + j;
                 if (n >= (uint32_t)p.N) continue;
                 double *dst = p.c + ocm + spg_g2(p.cn, n);
                 const double y = spg_reads_out<OP>::value ? *dst : 0.0;
@@ -149,19 +154,37 @@ namespace {
 
 typedef void (*ContractFn)(ContractParams);
 
-template <bool FMA>
+template <bool FMA, int RM, int RN>
 ContractFn contract_kernel(int op) {
     switch (op) {
-        case OP_SORT_ONE: return spg_contract<OP_SORT_ONE, FMA>;
-        case OP_SORT_NEG: return spg_contract<OP_SORT_NEG, FMA>;
-        case OP_SORT_POW2: return spg_contract<OP_SORT_POW2, FMA>;
-        case OP_SORT_ANY: return spg_contract<OP_SORT_ANY, FMA>;
-        case OP_ACC_ONE: return spg_contract<OP_ACC_ONE, FMA>;
-        case OP_ACC_NEG: return spg_contract<OP_ACC_NEG, FMA>;
-        case OP_ACC_POW2: return spg_contract<OP_ACC_POW2, FMA>;
-        case OP_ACC_ANY: return spg_contract<OP_ACC_ANY, FMA>;
-        default: return spg_contract<OP_GEN, FMA>;
+        case OP_SORT_ONE: return spg_contract<OP_SORT_ONE, FMA, RM, RN>;
+        case OP_SORT_NEG: return spg_contract<OP_SORT_NEG, FMA, RM, RN>;
+        case OP_SORT_POW2: return spg_contract<OP_SORT_POW2, FMA, RM, RN>;
+        case OP_SORT_ANY: return spg_contract<OP_SORT_ANY, FMA, RM, RN>;
+        case OP_ACC_ONE: return spg_contract<OP_ACC_ONE, FMA, RM, RN>;
+        case OP_ACC_NEG: return spg_contract<OP_ACC_NEG, FMA, RM, RN>;
+        case OP_ACC_POW2: return spg_contract<OP_ACC_POW2, FMA, RM, RN>;
+        case OP_ACC_ANY: return spg_contract<OP_ACC_ANY, FMA, RM, RN>;
+        default: return spg_contract<OP_GEN, FMA, RM, RN>;
     }
+}
+
+// Threads per tile: GB300's FP64 units sit in the SM's four sub-partitions,
+// each a warp's home, so an SM needs several warps to use them all.  The
+// tile is fixed at 16 x 16 outputs; small problems (few tiles per SM) get
+// more threads per tile, each with fewer outputs.
+ContractFn pick_kernel(int op, bool fma, uint32_t ntiles, int sms, int *threads) {
+    const uint64_t want_warps = (uint64_t)sms * 8;
+    if ((uint64_t)ntiles * 2 >= want_warps) {
+        *threads = 64;
+        return fma ? contract_kernel<true, 2, 2>(op) : contract_kernel<false, 2, 2>(op);
+    }
+    if ((uint64_t)ntiles * 4 >= want_warps) {
+        *threads = 128;
+        return fma ? contract_kernel<true, 2, 1>(op) : contract_kernel<false, 2, 1>(op);
+    }
+    *threads = 256;
+    return fma ? contract_kernel<true, 1, 1>(op) : contract_kernel<false, 1, 1>(op);
 }
 
 thread_local int g_contract_error = 0;
@@ -247,16 +270,16 @@ int launch_contract(ContractParams &P, int mode, double factor, double acc_facto
     P.fac = spg_make_factor(factor, acc_factor);
     P.scale_a = P.alpha != 1.0;
     const int op = spg_choose_op(factor, acc_factor);
-    const ContractFn fn = mode ? contract_kernel<true>(op) : contract_kernel<false>(op);
-    int dev = 0, sms = 152, nb = 0;
+    int dev = 0, sms = 152, nb = 0, nt = 64;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 152;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)fn, SPG_CT_NT, 0) != cudaSuccess || nb < 1)
+    const ContractFn fn = pick_kernel(op, mode != 0, P.ntiles, sms, &nt);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)fn, nt, 0) != cudaSuccess || nb < 1)
         nb = 1;
     cudaGetLastError();
     const int grid = (int)std::min<int64_t>((int64_t)sms * nb, (int64_t)P.ntiles);
     void *args[] = {(void *)&P};
-    if (cudaLaunchKernel((const void *)fn, dim3(grid), dim3(SPG_CT_NT), args, 0, st) != cudaSuccess) {
+    if (cudaLaunchKernel((const void *)fn, dim3(grid), dim3(nt), args, 0, st) != cudaSuccess) {
         cudaGetLastError();
         return SPAGHETTY_ERR_CUDA;
     }

@@ -27,11 +27,14 @@ def t2_8_oracle(t, v, d):
 
 
 @pytest.mark.parametrize("d", [(16, 16, 16, 16, 16, 16), (3, 5, 7, 2, 6, 5), (5, 7, 3, 9, 11, 3),
-                               (17, 2, 9, 4, 1, 33), (1, 1, 1, 1, 1, 1)])
+                               (17, 2, 9, 4, 1, 33), (1, 1, 1, 1, 1, 1), (18, 18, 17, 18, 3, 5),
+                               (24, 24, 24, 24, 8, 9)])
 def test_ccsd_t2_8_host_buffers_bits(cuda, d):
     """The Fortran drop-in on host arrays (staged through the device), the
     skeleton's shapes with tiles that are not multiples of the kernel's
-    16 x 16 x 32 blocking."""
+    16 x 16 x 32 blocking; on 152 SMs the tile counts (up to 256, 420 and
+    1296) select each of the three thread shapes (256, 128 and 64 threads
+    per tile)."""
     from spaghetty_gb300.contract import ccsd_t2_8
     d1, d2, d3, d4, d5, d6 = d
     rng = np.random.default_rng(sum(d))
