@@ -712,6 +712,30 @@ def run_contract(args, dev):
     return res
 
 
+def run_contract_case(args):
+    """One fused ccsd_t2_8 contraction at d^6 (profiling workload):
+    --contract-case D:MODE (MODE exact or fma)."""
+    import torch
+    from spaghetty_gb300.contract import contract_4x4
+    d_s, mode = args.contract_case.split(":")
+    d = int(d_s)
+    dev = torch.device("cuda", 0)
+    n = d ** 4
+    t = torch.rand(n, dtype=torch.float64, device=dev) - 0.5
+    v = torch.rand(n, dtype=torch.float64, device=dev) - 0.5
+    c = torch.empty(n, dtype=torch.float64, device=dev)
+    dims = (d, d, d, d)
+
+    def fn():
+        contract_4x4(t, dims, (4, 3, 2, 1), v, dims, (2, 1, 4, 3), c, (2, 1, 4, 3), mode=mode)
+
+    for _ in range(args.warmup):
+        fn()
+    tm = _timed_events(fn, args.steps, torch.cuda.current_stream(dev))
+    print(json.dumps({"contract_case": args.contract_case, "ms": round(tm * 1e3, 4),
+                      "gflops": round(2.0 * d ** 6 / tm / 1e9, 1)}), flush=True)
+
+
 def run_case(args):
     """One sort case, W warm-up + K timed launches (the profiling workload)."""
     import torch
@@ -785,6 +809,8 @@ def main():
     ap.add_argument("--batched-case", default=None,
                     help="N:E4LO-E4HI:E6LO-E6HI: time one reduced batched mix")
     ap.add_argument("--fused-case", default=None, help="GROUP:EXTENT: time one fused triples group")
+    ap.add_argument("--contract-case", default=None,
+                    help="D:MODE: time one fused ccsd_t2_8 contraction at D^6 (MODE exact|fma)")
     ap.add_argument("--case", default=None,
                     help="dims:perm:op[:factor] (op 0 sort, 1 sortacc; factor 0.5): time one case")
     ap.add_argument("--gpus", type=int, default=1)
@@ -804,6 +830,9 @@ def main():
         return
     if args.fused_case:
         run_fused_case(args)
+        return
+    if args.contract_case:
+        run_contract_case(args)
         return
     if args.batched_case:
         run_batched_case(args)
