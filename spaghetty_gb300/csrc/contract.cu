@@ -79,8 +79,11 @@ spg_contract(const __grid_constant__ ContractParams p) {
     constexpr int TMX = SPG_CT_TM / RM;             // threads along m
     constexpr int NT = TMX * (SPG_CT_TN / RN);
     constexpr int KROWS = NT / 16;                  // k rows one staging pass covers
-    __shared__ __align__(16) double As[SPG_CT_TK][SPG_CT_TM];
-    __shared__ __align__(16) double Bs[SPG_CT_TK][SPG_CT_TN];
+    constexpr int LPT = SPG_CT_TK / KROWS;          // staged elements per thread and operand
+    // two staging buffers: step s is computed from buffer s&1 while step
+    // s+1's operands travel from memory into the other
+    __shared__ __align__(16) double As[2][SPG_CT_TK][SPG_CT_TM];
+    __shared__ __align__(16) double Bs[2][SPG_CT_TK][SPG_CT_TN];
     const uint32_t tid = threadIdx.x;
     const uint32_t tx = tid % TMX, ty = tid / TMX;
     // staging: this thread loads tile row (tid & 15) at k rows (tid >> 4) + KROWS*j
@@ -93,37 +96,58 @@ spg_contract(const __grid_constant__ ContractParams p) {
         const bool lm_ok = m0 + lrow < (uint32_t)p.M, ln_ok = n0 + lrow < (uint32_t)p.N;
         const int64_t offa = lm_ok ? spg_g2(p.am, m0 + lrow) : 0;
         const int64_t offb = ln_ok ? spg_g2(p.bn, n0 + lrow) : 0;
+        // step k0's operands go straight from memory into buffer `buf` by
+        // 8-byte cp.async copies (zero-filled outside the tensors), so no
+        // registers hold them in flight
+        auto fetch = [&](int32_t k0, int buf) {
+#pragma unroll
+            for (int j = 0; j < LPT; ++j) {
+                const uint32_t kk = lk + (uint32_t)KROWS * j;
+                const uint32_t k = (uint32_t)k0 + kk;
+                const bool kin = k < (uint32_t)p.K;
+                const bool a_ok = kin && lm_ok, b_ok = kin && ln_ok;
+                spg_cp_async8((uint32_t)__cvta_generic_to_shared(&As[buf][kk][lrow]),
+                              a_ok ? p.a + offa + spg_g2(p.ak, k) : p.a, a_ok ? 8u : 0u);
+                spg_cp_async8((uint32_t)__cvta_generic_to_shared(&Bs[buf][kk][lrow]),
+                              b_ok ? p.b + offb + spg_g2(p.bk, k) : p.b, b_ok ? 8u : 0u);
+            }
+            spg_cp_commit();
+        };
+        // the loop's alpha*a(k,i), rounded once per element: each thread
+        // scales the elements it copied, after they landed
+        auto scale = [&](int buf) {
+            if (!p.scale_a) return;
+#pragma unroll
+            for (int j = 0; j < LPT; ++j) {
+                double *q = &As[buf][lk + (uint32_t)KROWS * j][lrow];
+                *q = __dmul_rn(p.alpha, *q);
+            }
+        };
         double acc[RM][RN];
 #pragma unroll
         for (int i = 0; i < RM; ++i)
 #pragma unroll
             for (int j = 0; j < RN; ++j) acc[i][j] = 0.0;
-        for (int32_t k0 = 0; k0 < p.K; k0 += SPG_CT_TK) {
-            __syncthreads();                // the previous step's tiles are consumed
-#pragma unroll
-            for (int j = 0; j < SPG_CT_TK / KROWS; ++j) {
-                const uint32_t kk = lk + (uint32_t)KROWS * j;
-                const uint32_t k = (uint32_t)k0 + kk;
-                double va = 0.0, vb = 0.0;
-                if (k < (uint32_t)p.K) {
-                    if (lm_ok) {
-                        va = __ldg(p.a + offa + spg_g2(p.ak, k));
-                        if (p.scale_a) va = __dmul_rn(p.alpha, va);
-                    }
-                    if (ln_ok) vb = __ldg(p.b + offb + spg_g2(p.bk, k));
-                }
-                As[kk][lrow] = va;
-                Bs[kk][lrow] = vb;
+        __syncthreads();                    // the previous tile's last step is consumed
+        fetch(0, 0);
+        int buf = 0;
+        for (int32_t k0 = 0; k0 < p.K; k0 += SPG_CT_TK, buf ^= 1) {
+            if (k0 + SPG_CT_TK < p.K) {
+                fetch(k0 + SPG_CT_TK, buf ^ 1);
+                spg_cp_wait<1>();           // this thread's copies of step k0 landed
+            } else {
+                spg_cp_wait<0>();
             }
-            __syncthreads();
+            scale(buf);
+            __syncthreads();                // ... and everyone else's
             const int32_t kn = min(SPG_CT_TK, p.K - k0);
             // k strictly ascending: the loop's order of additions
             for (int32_t kk = 0; kk < kn; ++kk) {
                 double av[RM], bv[RN];
 #pragma unroll
-                for (int i = 0; i < RM; ++i) av[i] = As[kk][RM * tx + i];
+                for (int i = 0; i < RM; ++i) av[i] = As[buf][kk][RM * tx + i];
 #pragma unroll
-                for (int j = 0; j < RN; ++j) bv[j] = Bs[kk][RN * ty + j];
+                for (int j = 0; j < RN; ++j) bv[j] = Bs[buf][kk][RN * ty + j];
 #pragma unroll
                 for (int i = 0; i < RM; ++i)
 #pragma unroll
@@ -131,6 +155,7 @@ spg_contract(const __grid_constant__ ContractParams p) {
                         acc[i][j] = FMA ? __fma_rn(av[i], bv[j], acc[i][j])
                                         : __dadd_rn(acc[i][j], __dmul_rn(av[i], bv[j]));
             }
+            __syncthreads();                // buffer buf is refilled two steps on
         }
         // each result element written once, at its sorted position
 #pragma unroll
