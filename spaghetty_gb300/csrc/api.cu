@@ -248,17 +248,20 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         rc = spg_build_params(pl, f, g);
         if (rc) return rc;
         if (want_tma) {
-            // The tuner times sorts with f = 0.5, so a plain sort (f = 1) of
-            // a large array on a tuned TMA plan runs that same kernel, as
-            // f = 2^0 on the power-of-two path (the same bits for every
-            // input but NaN, whose payload is not part of the contract).
-            // Measured on GB300: the bare shared-memory copy is 15-20%
-            // slower on the plans tuned at 100^4 (f = 1 sorts 5729 -> 6222
-            // GB/s on the sweep), but 2-4% faster on those tuned at 30^4
-            // and 50^4, whose arrays fit twice in L2; on untuned default
-            // plans neither is faster overall (0.93-1.08 across 50^4..100^4
-            // and 12^6..20^6).
-            if (pl->op == OP_SORT_ONE && fo.nelem >= SPG_TUNED_ONE_AS_POW2) pl->op = OP_SORT_POW2;
+            // The tuner times with f = 0.5, so a sort with f = 1 or -1 (and
+            // a sortacc with f = -1) of a large array on a tuned TMA plan
+            // runs that same kernel, as f = +-2^0 on the power-of-two path
+            // (the same bits for every input but NaN, whose payload is not
+            // part of the contract).  Measured on GB300: the bare
+            // shared-memory copy of f = 1 is 15-20% slower on the plans
+            // tuned at 100^4 (f = 1 sorts 5729 -> 6222 GB/s on the sweep),
+            // but 2-4% faster on those tuned at 30^4 and 50^4, whose arrays
+            // fit twice in L2; on untuned default plans neither is faster
+            // overall (0.93-1.08 across 50^4..100^4 and 12^6..20^6).
+            if (fo.nelem >= SPG_TUNED_ONE_AS_POW2) {
+                if (pl->op == OP_SORT_ONE || pl->op == OP_SORT_NEG) pl->op = OP_SORT_POW2;
+                if (pl->op == OP_ACC_NEG) pl->op = OP_ACC_POW2;
+            }
             return to_tma(pl, ov.threads, ov.ept, ov.stages - 10, true);
         }
         return SPAGHETTY_OK;

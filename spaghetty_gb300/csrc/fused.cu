@@ -69,7 +69,7 @@ __device__ __forceinline__ double spg_fused_add(double acc, double x, const SpgF
 __device__ __forceinline__ double spg_fused_apply(int op, double acc, double x, const SpgFactor &F) {
     switch (op) {
         case OP_ACC_ONE: return spg_fused_add<OP_ACC_ONE>(acc, x, F);
-        case OP_ACC_NEG: return spg_fused_add<OP_ACC_NEG>(acc, x, F);
+        case OP_ACC_NEG: return __dsub_rn(acc, x);   // acc + x*(-1): one rounding
         case OP_ACC_POW2: return spg_fused_add<OP_ACC_POW2>(acc, x, F);
         default: return spg_fused_add<OP_ACC_ANY>(acc, x, F);
     }

@@ -118,9 +118,9 @@ SpgFactor spg_make_factor(double f, double g) {
     F.g = g;
     int k = 0;
     const int fc = factor_class(f, &k);
-    // f = 1 gets the fields of 2^0 too: the TMA-staged kernel runs plain
-    // sorts on the power-of-two path
-    if (fc == 0 || fc == 2) {
+    // f = 1 and f = -1 get the fields of +-2^0 too: tuned TMA-staged plans
+    // of large arrays run them on the power-of-two path
+    if (fc <= 2) {
         F.k = k;
         F.sgn_hi = std::signbit(f) ? 0x80000000u : 0u;
         // biased exponents e of x with 1 <= e <= 2046 and 1 <= e + k <= 2046
