@@ -85,3 +85,42 @@ def test_contract_chain_matches_einsum(seed):
                              out=y.copy())
         want = g * y + f * 0.75 * c_ref
         np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-12)
+
+
+def test_contract_entry_validates_arguments_on_host():
+    """The C ABI checks shapes, permutations and the mode before touching
+    any memory or the GPU (no CUDA device needed)."""
+    import ctypes
+
+    from spaghetty_gb300._lib import int_array, lib
+    L = lib()
+    d4 = int_array((4, 4, 4, 4))
+    ok = int_array((1, 2, 3, 4))
+    buf = np.zeros(256)
+    p = ctypes.c_void_p(buf.ctypes.data)
+
+    def call(dims_b=d4, perm_a=ok, mode=0, a=p):
+        return L.spaghetty_contract_4x4(a, d4, perm_a, p, dims_b, ok, p, ok, 1.0, 1.0, 0.0, mode,
+                                        None)
+    assert call(mode=5) == 9                                   # SPAGHETTY_ERR_CONFIG
+    assert call(perm_a=int_array((1, 2, 2, 4))) == 2           # SPAGHETTY_ERR_PERM
+    assert call(dims_b=int_array((4, 4, 3, 4))) == 3           # contracted dims differ
+    assert call(dims_b=int_array((4, 0, 4, 4))) == 3           # a zero extent
+    assert call(a=None) == 5                                   # SPAGHETTY_ERR_NULL
+    assert L.spaghetty_contract_last_error() == 5
+    big = int_array((1 << 16, 1 << 16, 1, 1))
+    assert L.spaghetty_contract_4x4(p, big, ok, p, big, ok, p, ok, 1.0, 1.0, 0.0, 0, None) == 4
+
+
+def test_ccsd_t2_8_checks_sizes_on_host():
+    import ctypes
+
+    from spaghetty_gb300._lib import lib
+    ir = lambda v: ctypes.byref(ctypes.c_int(v))   # noqa: E731
+    buf = np.zeros(16)
+    p = ctypes.c_void_p(buf.ctypes.data)
+    # dims 2 each: every tensor holds 16 elements; size_c one short
+    rc = lib().ccsd_t2_8_status(p, ir(16), p, ir(16), p, ir(15), *[ir(2)] * 6)
+    assert rc == 3
+    rc = lib().ccsd_t2_8_status(p, ir(16), p, ir(16), p, ir(16), *[ir(2)] * 5, ir(0))
+    assert rc == 3
