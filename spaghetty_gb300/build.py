@@ -4,7 +4,7 @@ Makefiles, trunk/makelib.py:39-97, trunk/generator2.py:745-906).
 Emits the kernel variant tables (generator.py), compiles every translation
 unit for sm_103a in parallel with nvcc, and links the in-tree shared library
 ``spaghetty_gb300/libspaghetty_gb300.so`` (CUDA runtime linked statically, so
-the library depends on nothing but the driver).
+the library depends on nothing but the NVIDIA driver).
 """
 from __future__ import annotations
 

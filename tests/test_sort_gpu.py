@@ -68,7 +68,7 @@ def test_golden_digests_all_perms(cuda):
 
 @pytest.mark.parametrize("acc", [False, True])
 def test_sort4_plain_30(cuda, acc):
-    """configs[0]: 30^4, b(i,j,k,l) = f*a(l,k,j,i), f = -0.5, every perm."""
+    """The plain 30^4 workload, b(i,j,k,l) = f*a(l,k,j,i) with f = -0.5, for every perm."""
     dims = (30, 30, 30, 30)
     n = 30 ** 4
     u = O.seeded_uniform(n, 1)
