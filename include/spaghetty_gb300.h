@@ -406,6 +406,15 @@ int spaghetty_contract_4x4(const double *a, const int *dims_a, const int *perm_a
 /* The last SPAGHETTY_* code of the contraction entries on this thread. */
 int spaghetty_contract_last_error(void);
 
+/* Host replay of the contraction kernel's index arithmetic for one problem
+ * (no GPU needed): every operand element is read for exactly the (m, k) or
+ * (n, k) it holds and inside its tensor, and every result element is written
+ * exactly once, under each of the kernel's three thread shapes.  stats (4
+ * int64, may be NULL): M, N, K, tiles.  SPAGHETTY_ERR_CONFIG on a violation,
+ * SPAGHETTY_ERR_TOO_LARGE above 2^28 elements per tensor. */
+int spaghetty_contract_verify(const int *dims_a, const int *perm_a, const int *dims_b,
+                              const int *perm_b, const int *perm_c, int64_t *stats);
+
 /* The macaroni skeleton's subroutine, drop-in
  * (ccsd_t2_8_skeleton.F:174-184): i0(p3,p4,h1,h2) = Sum(p5,p6)
  * v(p3,p4,p5,p6) * t(p5,p6,h1,h2) with a_raw = t of dims (dim5,dim6,dim1,

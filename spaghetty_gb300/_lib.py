@@ -120,6 +120,8 @@ PROTOTYPES = {
                                               ctypes.c_double, ctypes.c_double, ctypes.c_double,
                                               ctypes.c_int, ctypes.c_void_p]),
     "spaghetty_contract_last_error": (ctypes.c_int, []),
+    "spaghetty_contract_verify": (ctypes.c_int, [c_int_p, c_int_p, c_int_p, c_int_p, c_int_p,
+                                                 ctypes.POINTER(ctypes.c_int64)]),
     "ccsd_t2_8": (None, _T2_8), "ccsd_t2_8_": (None, _T2_8),
     "ccsd_t2_8_status": (ctypes.c_int, _T2_8),
     "spaghetty_selftest": (ctypes.c_int, []),

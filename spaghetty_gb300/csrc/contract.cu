@@ -38,6 +38,7 @@
 #include <algorithm>
 #include <map>
 #include <mutex>
+#include <vector>
 
 #include "kernels.cuh"
 #include "plan.h"
@@ -67,7 +68,9 @@ struct ContractParams {
     SpgFactor fac;
 };
 
-__device__ __forceinline__ int64_t spg_g2(const SpgGroup2 &g, uint32_t x) {
+// Host-callable too, so that spaghetty_contract_verify replays the kernel's
+// own index arithmetic on the CPU.
+SPG_HD int64_t spg_g2(const SpgGroup2 &g, uint32_t x) {
     const uint32_t x0 = fd_div(x, g.e1);
     return (int64_t)x0 * g.w0 + (int64_t)(x - x0 * g.e1v) * g.w1;
 }
@@ -436,9 +439,77 @@ void t2_8_void(const double *a_raw, const int *size_a, const double *b_raw, cons
     }
 }
 
+// Replays, on the host, every address the kernel forms for one problem:
+// the operand element (m, k) / (n, k) that each staging copy reads and the
+// result element (m, n) that each thread writes, with the tile walk and the
+// thread-to-output map of each of the three thread shapes.  Every operand
+// element must be read for exactly the (m, k) it holds, inside the tensor;
+// every result element written exactly once.
+template <int RM, int RN>
+bool verify_writes(const ContractParams &P, int64_t nc, std::vector<uint8_t> &seen) {
+    constexpr int TMX = SPG_CT_TM / RM, NT = TMX * (SPG_CT_TN / RN);
+    std::fill(seen.begin(), seen.end(), 0);
+    for (uint32_t t = 0; t < P.ntiles; ++t) {
+        const uint32_t tn = fd_div(t, P.mtiles);
+        const uint32_t tm = t - tn * P.mtiles.d;
+        const uint32_t m0 = tm * SPG_CT_TM, n0 = tn * SPG_CT_TN;
+        for (uint32_t tid = 0; tid < (uint32_t)NT; ++tid) {
+            const uint32_t tx = tid % TMX, ty = tid / TMX;
+            for (int i = 0; i < RM; ++i)
+                for (int j = 0; j < RN; ++j) {
+                    const uint32_t m = m0 + RM * tx + i, n = n0 + RN * ty + j;
+                    if (m >= (uint32_t)P.M || n >= (uint32_t)P.N) continue;
+                    const int64_t o = spg_g2(P.cm, m) + spg_g2(P.cn, n);
+                    if (o < 0 || o >= nc || seen[(size_t)o]++) return false;
+                }
+        }
+    }
+    for (int64_t o = 0; o < nc; ++o)
+        if (seen[(size_t)o] != 1) return false;
+    return true;
+}
+
+bool verify_operand(const SpgGroup2 &rows, const SpgGroup2 &ks, uint32_t R, uint32_t K, int64_t n,
+                    std::vector<uint8_t> &seen) {
+    seen.assign((size_t)n, 0);
+    for (uint32_t r = 0; r < R; ++r)
+        for (uint32_t k = 0; k < K; ++k) {
+            const int64_t o = spg_g2(rows, r) + spg_g2(ks, k);
+            if (o < 0 || o >= n || seen[(size_t)o]++) return false;
+        }
+    return true;
+}
+
 }  // namespace
 
 extern "C" {
+
+int spaghetty_contract_verify(const int *dims_a, const int *perm_a, const int *dims_b,
+                              const int *perm_b, const int *perm_c, int64_t *stats) {
+    ContractParams P;
+    memset(&P, 0, sizeof(P));
+    int64_t na, nb, nc;
+    int rc = contract_params(dims_a, perm_a, dims_b, perm_b, perm_c, &P, &na, &nb, &nc);
+    if (rc) return rc;
+    if (na > (int64_t(1) << 28) || nb > (int64_t(1) << 28) || nc > (int64_t(1) << 28))
+        return SPAGHETTY_ERR_TOO_LARGE;
+    std::vector<uint8_t> seen;
+    if (!verify_operand(P.am, P.ak, (uint32_t)P.M, (uint32_t)P.K, na, seen) ||
+        !verify_operand(P.bn, P.bk, (uint32_t)P.N, (uint32_t)P.K, nb, seen))
+        return SPAGHETTY_ERR_CONFIG;
+    seen.assign((size_t)nc, 0);
+    if (!verify_writes<2, 2>(P, nc, seen) || !verify_writes<2, 1>(P, nc, seen) ||
+        !verify_writes<1, 1>(P, nc, seen))
+        return SPAGHETTY_ERR_CONFIG;
+    if (stats) {
+        stats[0] = P.M;
+        stats[1] = P.N;
+        stats[2] = P.K;
+        stats[3] = P.ntiles;
+    }
+    return SPAGHETTY_OK;
+}
+
 
 int spaghetty_contract_4x4(const double *a, const int *dims_a, const int *perm_a, const double *b,
                            const int *dims_b, const int *perm_b, double *c, const int *perm_c,

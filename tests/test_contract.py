@@ -124,3 +124,48 @@ def test_ccsd_t2_8_checks_sizes_on_host():
     assert rc == 3
     rc = lib().ccsd_t2_8_status(p, ir(16), p, ir(16), p, ir(16), *[ir(2)] * 5, ir(0))
     assert rc == 3
+
+
+def _verify(da, pa, db, pb, pc):
+    import ctypes
+
+    from spaghetty_gb300._lib import int_array, lib
+    st = (ctypes.c_int64 * 4)()
+    rc = lib().spaghetty_contract_verify(int_array(da), int_array(pa), int_array(db),
+                                         int_array(pb), int_array(pc), st)
+    return rc, list(st)
+
+
+def test_contract_verify_replays_kernel_addresses():
+    """spaghetty_contract_verify replays the kernel's own index arithmetic on
+    the CPU (operand reads, tile walk, result writes under every thread
+    shape) for the skeleton's shapes and 300 random problems."""
+    for d in [(16,) * 6, (3, 5, 7, 2, 6, 5), (17, 2, 9, 4, 1, 33), (18, 18, 17, 18, 3, 5),
+              (1, 1, 1, 1, 1, 1)]:
+        d1, d2, d3, d4, d5, d6 = d
+        rc, st = _verify((d5, d6, d1, d2), (4, 3, 2, 1), (d3, d4, d5, d6), (2, 1, 4, 3), (2, 1, 4, 3))
+        assert rc == 0 and st[:3] == [d1 * d2, d3 * d4, d5 * d6], (d, rc, st)
+    rng = np.random.default_rng(77)
+    for _ in range(300):
+        pa = tuple(int(x) + 1 for x in rng.permutation(4))
+        pb = tuple(int(x) + 1 for x in rng.permutation(4))
+        pc = tuple(int(x) + 1 for x in rng.permutation(4))
+        sa = [int(x) for x in rng.integers(1, 40, 4)]
+        sb = [int(x) for x in rng.integers(1, 40, 2)] + sa[2:]
+        da, db = [0] * 4, [0] * 4
+        for q in range(4):
+            da[pa[q] - 1] = sa[q]
+            db[pb[q] - 1] = sb[q]
+        rc, st = _verify(da, pa, db, pb, pc)
+        assert rc == 0, (da, pa, db, pb, pc, rc)
+        assert st[3] == -(-st[0] // 16) * -(-st[1] // 16)
+
+
+def test_contract_verify_refuses_bad_shapes():
+    assert _verify((4, 4, 4, 4), (1, 2, 3, 4), (4, 4, 5, 4), (1, 2, 3, 4), (1, 2, 3, 4))[0] == 3
+    assert _verify((4, 4, 4, 4), (1, 2, 3, 3), (4, 4, 4, 4), (1, 2, 3, 4), (1, 2, 3, 4))[0] == 2
+    # 2^29 elements in a: beyond the replay's limit (13); 2^60 result tiles: overflow (4)
+    assert _verify((1 << 15, 1 << 14, 1, 1), (1, 2, 3, 4), (4, 4, 1, 1), (1, 2, 3, 4),
+                   (1, 2, 3, 4))[0] == 13
+    assert _verify((1 << 15,) * 2 + (1, 1), (1, 2, 3, 4), (1 << 15,) * 2 + (1, 1), (1, 2, 3, 4),
+                   (1, 2, 3, 4))[0] == 4
