@@ -625,6 +625,7 @@ int sort_host_pipelined(int rank, const double *u, double *s, const int *dims, c
 
 int sort_sync(int rank, const double *u, double *s, const int *dims, const int *perm,
               double f, double g) {
+    SpgRange range(g == 0.0 ? "tce_sort" : "tce_sortacc");
     Folded fo;
     int rc = spg_fold(rank, dims, perm, &fo);
     if (rc) return rc;
@@ -895,6 +896,7 @@ int spaghetty_selftest(void) { return spg_selftest_host(); }
 
 int spaghetty_sort_async(int rank, const double *unsorted, double *sorted, const int *dims,
                          const int *perm, double factor, double acc_factor, void *stream) {
+    SpgRange range("spaghetty_sort_async");
     Folded fo;
     int rc = spg_fold(rank, dims, perm, &fo);
     if (rc) return record(rc);

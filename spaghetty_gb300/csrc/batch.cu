@@ -412,6 +412,7 @@ int spaghetty_batch_tune_set(int rank, int ext_lo, int ext_hi, int run_in, int r
 }
 
 int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
+    SpgRange range("spaghetty_batch_launch");
     if (!b) return SPAGHETTY_ERR_NULL;
     cudaStream_t st = (cudaStream_t)stream;
     if (!b->direct.empty()) {
@@ -454,6 +455,7 @@ int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
 }
 
 int spaghetty_batch_launch_plain(spaghetty_batch *b, void *stream) {
+    SpgRange range("spaghetty_batch_launch_plain");
     if (!b) return SPAGHETTY_ERR_NULL;
     int cur = -1;
     if (cudaGetDevice(&cur) != cudaSuccess) cudaGetLastError();

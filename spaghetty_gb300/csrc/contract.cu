@@ -415,6 +415,7 @@ int contract_sync(const double *a, const int *dims_a, const int *perm_a, const d
 int t2_8(const double *a_raw, const int *size_a, const double *b_raw, const int *size_b,
          double *c_done, const int *size_c, const int *d1, const int *d2, const int *d3,
          const int *d4, const int *d5, const int *d6) {
+    SpgRange range("ccsd_t2_8");
     if (!size_a || !size_b || !size_c || !d1 || !d2 || !d3 || !d4 || !d5 || !d6)
         return SPAGHETTY_ERR_NULL;
     const int dims_a[4] = {*d5, *d6, *d1, *d2}, perm_a[4] = {4, 3, 2, 1};
@@ -514,6 +515,7 @@ int spaghetty_contract_verify(const int *dims_a, const int *perm_a, const int *d
 int spaghetty_contract_4x4(const double *a, const int *dims_a, const int *perm_a, const double *b,
                            const int *dims_b, const int *perm_b, double *c, const int *perm_c,
                            double alpha, double factor, double acc_factor, int mode, void *stream) {
+    SpgRange range("spaghetty_contract_4x4");
     if (mode != 0 && mode != 1) return crecord(SPAGHETTY_ERR_CONFIG);
     ContractParams P;
     memset(&P, 0, sizeof(P));

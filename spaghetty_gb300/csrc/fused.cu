@@ -880,6 +880,7 @@ static int fused_pass(int rank, int nsrc, const double *const *unsorted, const i
 extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *unsorted,
                                        const int *dims, const int *perms, const double *factors,
                                        double *sorted, void *stream) {
+    SpgRange range("spaghetty_sortacc_fused");
     if (rank < 1 || rank > SPG_FUSED_MAXR) return SPAGHETTY_ERR_RANK;
     if (nsrc < 1 || nsrc > SPG_FUSED_MAXS) return SPAGHETTY_ERR_CONFIG;
     if (!unsorted || !dims || !perms || !factors) return SPAGHETTY_ERR_NULL;

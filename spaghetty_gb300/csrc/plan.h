@@ -12,6 +12,7 @@
 // order (coalesced), and writes it in output order (coalesced).
 #pragma once
 #include <stdint.h>
+#include <nvtx3/nvToolsExt.h>
 
 #define SPG_MAXR 8
 
@@ -154,6 +155,17 @@ struct Plan {
     int smem_bytes;
     int64_t wf_pad0, wf_ideal; // store-phase shared wavefronts: unpadded tile, conflict-free
     KParams kp;
+};
+
+// An NVTX range around one library entry (header-only NVTX 3: a few
+// nanoseconds when no profiler is attached), so that timelines name the
+// library's host calls: the synchronous sorts, the batched launches, the
+// fused sortacc and the fused contraction.
+struct SpgRange {
+    explicit SpgRange(const char *name) { nvtxRangePushA(name); }
+    ~SpgRange() { nvtxRangePop(); }
+    SpgRange(const SpgRange &) = delete;
+    SpgRange &operator=(const SpgRange &) = delete;
 };
 
 // Host-side planning (plan.cpp).  All return a SPAGHETTY_* status.
