@@ -34,12 +34,16 @@ def contract_4x4(a, dims_a, perm_a, b, dims_b, perm_b, c, perm_c, alpha=1.0, fac
     on CUDA FP64 tensors, queued on torch's current stream (or ``stream``).
     ``mode`` "exact" adds the products in k order with every product and sum
     rounded (the skeleton's loop_dgemm bits); "fma" uses fused multiply-adds."""
+    _, _, _, dims_c = contract_shapes(dims_a, perm_a, dims_b, perm_b, perm_c)
     for t in (a, b, c):
         if t.dtype != torch.float64 or not t.is_cuda or not t.is_contiguous():
             raise TypeError("operands must be contiguous CUDA FP64 tensors")
-    _, _, _, dims_c = contract_shapes(dims_a, perm_a, dims_b, perm_b, perm_c)
-    if c.numel() != int(torch.tensor(dims_c).prod()):
-        raise ValueError("result has %d elements, the contraction gives %s" % (c.numel(), dims_c))
+    for t, dims, name in ((a, dims_a, "a"), (b, dims_b, "b"), (c, dims_c, "c")):
+        n = 1
+        for d in dims:
+            n *= int(d)
+        if t.numel() != n:
+            raise ValueError("%s has %d elements, its dims %s need %d" % (name, t.numel(), tuple(dims), n))
     if stream is None:
         stream = torch.cuda.current_stream(c.device).cuda_stream
     rc = lib().spaghetty_contract_4x4(
@@ -56,6 +60,11 @@ def ccsd_t2_8(a_raw, b_raw, c_done, dims: Sequence[int]):
     (d3,d4,d1,d2)) = sum over (p5,p6) of b_raw (d3,d4,d5,d6) times a_raw
     (d5,d6,d1,d2); host (numpy) or device (torch) buffers, synchronous."""
     d1, d2, d3, d4, d5, d6 = (int(x) for x in dims)
+    for t, need, name in ((a_raw, d5 * d6 * d1 * d2, "a_raw"), (b_raw, d3 * d4 * d5 * d6, "b_raw"),
+                          (c_done, d1 * d2 * d3 * d4, "c_done")):
+        n = t.numel() if isinstance(t, torch.Tensor) else t.size
+        if n < need:
+            raise ValueError("%s has %d elements, the dims need %d" % (name, n, need))
 
     def ptr(t):
         return ctypes.c_void_p(t.data_ptr() if isinstance(t, torch.Tensor) else t.ctypes.data)

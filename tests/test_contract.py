@@ -169,3 +169,19 @@ def test_contract_verify_refuses_bad_shapes():
                    (1, 2, 3, 4))[0] == 13
     assert _verify((1 << 15,) * 2 + (1, 1), (1, 2, 3, 4), (1 << 15,) * 2 + (1, 1), (1, 2, 3, 4),
                    (1, 2, 3, 4))[0] == 4
+
+
+def test_python_wrappers_check_buffer_sizes():
+    """The C ABI cannot see buffer sizes; the Python wrappers check them
+    against the dims before any call (no GPU needed: they raise first)."""
+    import torch
+
+    from spaghetty_gb300.contract import ccsd_t2_8, contract_4x4
+    with pytest.raises(ValueError):
+        ccsd_t2_8(np.zeros(15), np.zeros(16), np.zeros(16), (2,) * 6)
+    with pytest.raises(ValueError):
+        ccsd_t2_8(np.zeros(16), np.zeros(16), np.zeros(8), (2,) * 6)
+    with pytest.raises(ValueError):   # contracted dims differ
+        contract_4x4(torch.zeros(16, dtype=torch.float64), (2, 2, 2, 2), (1, 2, 3, 4),
+                     torch.zeros(24, dtype=torch.float64), (2, 2, 3, 2), (1, 2, 3, 4),
+                     torch.zeros(16, dtype=torch.float64), (1, 2, 3, 4))
