@@ -234,7 +234,10 @@ int spaghetty_set_option(int option, int value);
 /* Synchronise the current device and report (then clear) the kernels'
  * status word: SPAGHETTY_ERR_DEVICE if a kernel gave up a bounded wait (its
  * pipeline's transfers did not arrive in time), else SPAGHETTY_OK.  The
- * synchronous entry points check it themselves. */
+ * synchronous entry points check it themselves.  The word is process-wide:
+ * one word for every device, stream and host thread, so a timed-out wait in
+ * one stream's kernel is reported (and cleared) by whichever synchronous
+ * call or spaghetty_device_status() reads it next. */
 int spaghetty_device_status(void);
 
 /* ---- plans (host only, no GPU needed) --------------------------------- */
@@ -253,7 +256,9 @@ typedef struct spaghetty_plan_info {
     int64_t ntiles;     /* number of boxes covering the tensor            */
     int run_in;         /* contiguous input elements per box row          */
     int run_out;        /* contiguous output elements per box row         */
-    int pad_period;     /* shared-memory padding: one word every N (0=none) */
+    int pad_period;     /* shared-memory bank-conflict avoidance: kinds 2/3,
+                           padding of one word every N; kind 4, the step of
+                           the permute step's diagonal skew (0 = none) */
     int masked;         /* 1 when boundary boxes need element masks      */
     int grid;           /* CTAs launched                                  */
     int vec;            /* 2 when 16-byte vector accesses are used        */
@@ -314,6 +319,17 @@ int spaghetty_selftest(void);
 int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *unsorted,
                             const int *dims, const int *perms, const double *factors,
                             double *sorted, void *stream);
+
+/* The same with the first term overwriting: sorted = factors[0] *
+ * permute_{perms[0]}(unsorted[0]), then the sortaccs of k = 1..nsrc-1 --
+ * bit-identical to one tce_sort call followed by nsrc-1 tce_sortacc calls
+ * (trunk/old_sort.f:33-95 then :512-575; a zero-filled start would turn a
+ * -0.0 first product into +0.0), without reading `sorted`.  Sources may
+ * repeat (y = sum_k f_k * permute_k(x), the differentiable sort's forward
+ * and backward).  Same arguments and limits as spaghetty_sortacc_fused. */
+int spaghetty_sort_fused(int rank, int nsrc, const double *const *unsorted,
+                         const int *dims, const int *perms, const double *factors,
+                         double *sorted, void *stream);
 
 /* ---- batched work lists (one persistent launch for many sorts) -------- */
 
@@ -394,7 +410,9 @@ int spaghetty_batch_tune_set(int rank, int ext_lo, int ext_hi, int run_in, int r
  * as tce_sort_4 / tce_sortacc_4 of c_sort round them.  mode 0: k ascending,
  * every product and sum rounded -- the bits of the skeleton's loop_dgemm
  * case 3 (ccsd_t2_8_skeleton.F:214-292) on a zeroed c_sort; mode 1: the
- * same order with fused multiply-adds (faster, not bit-identical).  Dims
+ * same order with fused multiply-adds (faster, not bit-identical); mode 2:
+ * the products summed by FP64 matrix instructions (mma.sync .f64, within
+ * rounding like mode 1).  Dims
  * and perms are 4 ints each (1-based perms); the operands must agree on the
  * contracted dims (else SPAGHETTY_ERR_DIMS).  Device (or managed) memory of
  * one device, else SPAGHETTY_ERR_MEMSPACE; asynchronous on `stream`. */
@@ -435,25 +453,30 @@ int ccsd_t2_8_status(const double *a_raw, const int *size_a, const double *b_raw
                      const int *dim2, const int *dim3, const int *dim4, const int *dim5,
                      const int *dim6);
 
-/* Batched sorts for callers that cannot allocate device memory -- code
- * running while a CUDA graph is being captured (where cudaMalloc is not
- * allowed), or inside an application that owns the whole device memory
- * budget.  No counterpart in the reference (its sorts are host loops that
- * need no scratch).  Runs the same persistent batched kernel as
+/* Batched sorts for callers that cannot allocate device memory -- an
+ * application that has handed the whole device memory to its own pool
+ * allocator (a library's cudaMalloc would then fail or escape its
+ * accounting), or code that must not cause the device-wide synchronisation
+ * cudaMalloc/cudaFree may trigger while other streams run.  No counterpart
+ * in the reference (its sorts are host loops that need no scratch).  Runs
+ * the same persistent batched kernel as
  * spaghetty_batch_launch, but the work list, unit counter and status word
  * live in a 4 MiB device array that is part of this library (every GPU that
  * loads it holds that array until exit); the caller passes only inputs and
  * outputs, and the call allocates nothing.  Limits: at most 1024 sorts, and
  * the work list must fit the 4 MiB: 896 bytes per sort plus 4 bytes per work
  * unit of ~16K elements (with 1024 sorts, about 819,000 units, i.e. some
- * 13 G elements); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The first call on a device looks up the array's
- * device address (set-up); make that first call before any stream capture.
- * Every call shares the one array, which keeps the previous call's contents:
- * the counter and status word are cleared on each call, the rest is
- * overwritten.  The call is synchronous on `stream` (it returns after the
- * sorts finish, with SPAGHETTY_ERR_DEVICE if a job failed the kernel's
- * checks); calls that overlap on the GPU (for instance from several
- * processes' streams sharing one context) would race on the array. */
+ * 13 G elements); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The first
+ * call on a device looks up the array's device address (set-up); make that
+ * first call before any stream capture.  Every call shares the one array,
+ * which keeps the previous call's contents: the counter and status word are
+ * cleared on each call, the rest is overwritten.  The call is synchronous on
+ * `stream` (it returns after the sorts finish, with SPAGHETTY_ERR_DEVICE if
+ * a job failed the kernel's checks).  Calls from several host threads are
+ * serialised by a lock and each waits for its kernel, so one loaded copy of
+ * the library does not run two at once; calls that did overlap on the GPU
+ * (a caller that ignores an error return and calls again while the failed
+ * call's kernel still runs) would race on the array. */
 int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries, int n, void *stream);
 
 /* Library version string. */

@@ -187,9 +187,12 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
     return rc;
 }
 
+int choose_skew(Plan *pl);
+
 // Switch a built tiled plan to the TMA-staged kernel with the given shape.
 int to_tma(Plan *pl, int threads, int ept, int stages, bool strict) {
     TmaLayout tl;
+    pl->sk_stride = pl->sk_len = pl->sk_mul = 0;
     if ((pl->kind != KIND_TILED && pl->kind != KIND_DIRECT) || threads * ept < pl->kp.vol ||
         spg_tma_layout(*pl, stages, &tl) != SPAGHETTY_OK ||
         tma_smem_bytes(tl, stages) > kMaxSmemPerBlock)
@@ -199,6 +202,75 @@ int to_tma(Plan *pl, int threads, int ept, int stages, bool strict) {
     pl->stages = stages;
     pl->kind = KIND_TMA;
     pl->smem_bytes = tma_smem_bytes(tl, stages);
+    choose_skew(pl);
+    return SPAGHETTY_OK;
+}
+
+// Shared-memory wavefronts of the TMA kernel's permute step under one slot
+// mapping: per half warp (16 consecutive slots of one element index k), the
+// 8-byte reads of the input tile at lin and the writes of the output tile at
+// e (a sortacc's reads of the old output use the same words as the writes).
+// A half warp's accesses take one wavefront per access of the busiest bank
+// pair (distinct words; equal words are one access).
+static int64_t tma_permute_wavefronts(const Plan &pl, const TmaParams &tp) {
+    const int NT = pl.threads, V = pl.kp.vol;
+    int64_t total = 0;
+    for (int k = 0; k < pl.ept; ++k)
+        for (int h = 0; h < NT / 16; ++h) {
+            uint32_t rd[16], wr[16];
+            int nw = 0;
+            for (int t = 0; t < 16; ++t) {
+                const uint32_t n = (uint32_t)(k * NT + h * 16 + t);
+                if (n >= (uint32_t)V) continue;
+                uint32_t e;
+                int32_t lin;
+                spg_tma_slot(pl.kp, tp, n, e, lin);
+                rd[nw] = (uint32_t)lin;
+                wr[nw] = e;
+                ++nw;
+            }
+            for (const uint32_t *w : {rd, wr}) {
+                int cnt[16] = {0}, worst = 0;
+                for (int a = 0; a < nw; ++a) {
+                    bool dup = false;
+                    for (int b = 0; b < a; ++b) dup = dup || w[b] == w[a];
+                    if (!dup) worst = std::max(worst, ++cnt[w[a] & 15u]);
+                }
+                total += worst;
+            }
+        }
+    return total;
+}
+
+// Pick the permute-step skew of a TMA plan: no skew, or a rotation of one
+// output dim's coordinate by (slot mod 16) * m for m in 1..3, whichever
+// takes the fewest simulated wavefronts (ties keep the simpler mapping).
+int choose_skew(Plan *pl) {
+    pl->sk_stride = pl->sk_len = pl->sk_mul = 0;
+    if (pl->kind != KIND_TMA || pl->kp.vol >= 65535 || pl->fo.P[pl->fo.rank - 1] == pl->fo.rank - 1)
+        return SPAGHETTY_OK;   // same-order tiles: the permute step is the identity
+    TmaParams tp;
+    std::memset(&tp, 0, sizeof(tp));
+    int64_t best = tma_permute_wavefronts(*pl, tp);
+    const int64_t ideal = 2 * (int64_t)((pl->kp.vol + 15) / 16);
+    const BoxWalk &w = pl->kp.st;
+    int32_t stride = 1;
+    for (int d = 0; d < w.n && best > ideal; ++d) {
+        const int32_t len = (int32_t)w.len[d].d;
+        for (int m = 1; m <= 3 && len > 1; ++m) {
+            tp.sk_stride = stride;
+            tp.sk_len = len;
+            tp.sk_mul = m;
+            const int64_t wf = tma_permute_wavefronts(*pl, tp);
+            if (wf < best) {
+                best = wf;
+                pl->sk_stride = stride;
+                pl->sk_len = len;
+                pl->sk_mul = m;
+            }
+        }
+        stride *= len;
+    }
     return SPAGHETTY_OK;
 }
 
@@ -948,7 +1020,7 @@ int spaghetty_plan_query(int rank, const int *dims, const int *perm, int op,
     out->ntiles = pl.kp.ntiles;
     out->run_in = pl.run_in;
     out->run_out = pl.run_out;
-    out->pad_period = pl.kp.pad;
+    out->pad_period = pl.kind == KIND_TMA ? pl.sk_mul : pl.kp.pad;
     out->masked = pl.masked;
     out->grid = 0;
     out->vec = 0;
@@ -975,6 +1047,18 @@ static int verify_tma(const Plan &pl, int64_t *stats) {
         int64_t s = 1;
         for (int d = R - 1; d >= 0; --d) { istr[d] = s; s *= fo.D[d]; }
     }
+    // the permute step's slots (spg_tma_slot, skew included) must cover
+    // every tile element exactly once; slot_in[e] = the input-tile element
+    // read for output-tile element e
+    std::vector<int32_t> slot_in((size_t)kp.vol, -1);
+    for (uint32_t s = 0; s < (uint32_t)kp.vol; ++s) {
+        uint32_t e;
+        int32_t lin;
+        spg_tma_slot(kp, tl.tp, s, e, lin);
+        if (e >= (uint32_t)kp.vol || slot_in[e] != -1) return SPAGHETTY_ERR_CONFIG;
+        if (tl.tp.sk_mul && (e > 0xFFFFu || lin < 0 || lin > 0xFFFF)) return SPAGHETTY_ERR_CONFIG;
+        slot_in[e] = lin;
+    }
     std::vector<int64_t> got((size_t)n, -1);
     int64_t writes = 0;
     for (uint32_t t = 0; t < kp.ntiles; ++t) {
@@ -996,10 +1080,7 @@ static int verify_tma(const Plan &pl, int64_t *stats) {
                 og += x * (int64_t)(tl.out_stride[m] / 8);
             }
             // input position of the element the permute step reads
-            int32_t a, b, lin;
-            uint32_t pk;
-            spg_walk(kp.st, e, a, b, lin, pk);
-            if (tl.tp.same_order) lin = (int32_t)e;
+            const int32_t lin = slot_in[e];
             if (lin < 0 || lin >= kp.vol) return SPAGHETTY_ERR_CONFIG;
             int64_t remi = lin, ig = 0;
             bool iin = true;

@@ -759,6 +759,9 @@ int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out) {
     out->tp.stage_bytes = (int32_t)(tile_al * (reads_out ? 2 : 1));
     out->tp.tx_bytes = (int32_t)(tile * (reads_out ? 2 : 1));
     out->tp.same_order = same_order ? 1 : 0;
+    out->tp.sk_stride = pl.sk_stride;
+    out->tp.sk_len = pl.sk_len;
+    out->tp.sk_mul = pl.sk_mul;
     (void)stages;
     return SPAGHETTY_OK;
 }

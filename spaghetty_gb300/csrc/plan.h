@@ -100,6 +100,11 @@ struct TmaParams {
     int32_t out_bytes;            // one output slot (two of them follow the stages)
     int32_t tx_bytes;             // bytes the loads of one box deliver
     int32_t same_order;           // 1: both maps list the dims in input order (identity permute)
+    // diagonal skew of the permute step (spg_tma_slot): slot n's output-tile
+    // coordinate y along one output dim (stride sk_stride in the output
+    // tile, box length sk_len) is moved to (y + (n mod 16) * sk_mul) mod
+    // sk_len; sk_mul = 0: no skew
+    int32_t sk_stride, sk_len, sk_mul;
     int *status;                  // error word (bounded waits that timed out)
 };
 
@@ -154,6 +159,7 @@ struct Plan {
     int grid;                 // filled at launch time
     int smem_bytes;
     int64_t wf_pad0, wf_ideal; // store-phase shared wavefronts: unpadded tile, conflict-free
+    int sk_stride, sk_len, sk_mul;   // TMA kernel: permute-step skew (TmaParams)
     KParams kp;
 };
 
@@ -205,3 +211,4 @@ int spg_selftest_host(void);
 // the plan cannot be expressed as 5-D tensor maps (odd stride-1 extents,
 // > 5 map dims, box > 256 along a map dim, ...).  stages: pipeline depth.
 int spg_tma_layout(const Plan &pl, int stages, TmaLayout *out);
+

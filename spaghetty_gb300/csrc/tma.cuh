@@ -106,6 +106,39 @@ __host__ __device__ __forceinline__ void spg_tma_coords(const KParams &p, const 
     }
 }
 
+// Permute-step slot n -> the output-tile element e it writes and the
+// input-tile element lin it reads.  Without skew e = n, so 16 consecutive
+// slots (a half warp's 8-byte accesses) write 16 consecutive words; but when
+// the input's stride-1 index lies along a slower output dim they read 16
+// words one input-tile row apart, and rows of 16, 32, 64... doubles put them
+// all in one bank pair (a 16-way conflict).  The skew moves the slot's
+// coordinate y along one output dim (stride sk_stride in the output tile,
+// box length sk_len) to (y + (lo mod 16) * sk_mul) mod sk_len, where lo =
+// n mod sk_stride holds the coordinates of the faster output dims: the shift
+// does not depend on y, so for each value of the other coordinates this is a
+// rotation of y and the slots still cover every element exactly once.  With
+// sk_stride a multiple of 16, lo mod 16 is the slot's lane in its half warp,
+// and the half warp's reads step along the input's stride-1 index into
+// different bank pairs (the host picks the dim and step by simulating the
+// banks).
+__host__ __device__ __forceinline__ void spg_tma_slot(const KParams &p, const TmaParams &tp, uint32_t n,
+                                                     uint32_t &e, int32_t &lin) {
+    e = n;
+    if (tp.sk_mul) {
+        const uint32_t lo = n % (uint32_t)tp.sk_stride;
+        const int32_t y = (int32_t)((n / (uint32_t)tp.sk_stride) % (uint32_t)tp.sk_len);
+        const int32_t y2 = (int32_t)((uint32_t)(y + (int32_t)(lo & 15u) * tp.sk_mul) % (uint32_t)tp.sk_len);
+        e = (uint32_t)((int32_t)n + (y2 - y) * tp.sk_stride);
+    }
+    if (tp.same_order) {
+        lin = (int32_t)e;
+        return;
+    }
+    int32_t a, b;
+    uint32_t pk;
+    spg_walk(p.st, e, a, b, lin, pk);
+}
+
 // Fetch a tensor map (kernel-parameter space) into the TMA unit's cache
 // ahead of its first use.
 __device__ __forceinline__ void spg_prefetch_tmap(const void *tmap) {
@@ -178,18 +211,21 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
             if (t < p.ntiles) { issue(t, q); ++issued; }
         }
     }
-    // permute-thread tables: output-tile element e = tid + k*NT takes
-    // input-tile element smr[k]
-    int32_t smr[EPT];
+    // permute-thread tables: slot n = tid + k*NT writes output-tile element
+    // e and reads input-tile element lin (spg_tma_slot).  Without skew e = n
+    // and tab[k] = lin; with skew tab[k] = e << 16 | lin (tiles hold at most
+    // 2^16 elements).  Unused slots hold SPG_INVALID.
+    const bool skew = tp.sk_mul != 0;
+    uint32_t tab[EPT];
 #pragma unroll
     for (int k = 0; k < EPT; ++k) {
-        const uint32_t e = tid + k * NT;
-        smr[k] = -1;
-        if (tid < NT && e < (uint32_t)p.vol) {
-            int32_t a, b, lin;
-            uint32_t pk;
-            spg_walk(p.st, e, a, b, lin, pk);
-            smr[k] = tp.same_order ? (int32_t)e : lin;
+        const uint32_t n = tid + k * NT;
+        tab[k] = SPG_INVALID;
+        if (tid < NT && n < (uint32_t)p.vol) {
+            uint32_t e;
+            int32_t lin;
+            spg_tma_slot(p, tp, n, e, lin);
+            tab[k] = skew ? (e << 16) | (uint32_t)lin : (uint32_t)lin;
         }
     }
     __syncthreads();                        // barriers initialised before anyone waits
@@ -253,12 +289,23 @@ spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
         const double *tin = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb);
         const double *told = reinterpret_cast<const double *>(smem_raw + (size_t)s * sb + in_bytes);
         double *tout = reinterpret_cast<double *>(smem_raw + out0 + (size_t)o * ob);
+        if (skew) {
 #pragma unroll
-        for (int k = 0; k < EPT; ++k) {
-            if (smr[k] >= 0) {
-                const uint32_t e = tid + k * NT;
-                const double y = spg_reads_out<OP>::value ? told[e] : 0.0;
-                tout[e] = spg_apply<OP>(tin[smr[k]], y, fac);
+            for (int k = 0; k < EPT; ++k) {
+                if (tab[k] != SPG_INVALID) {
+                    const uint32_t e = tab[k] >> 16;
+                    const double y = spg_reads_out<OP>::value ? told[e] : 0.0;
+                    tout[e] = spg_apply<OP>(tin[tab[k] & 0xFFFFu], y, fac);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < EPT; ++k) {
+                if (tab[k] != SPG_INVALID) {
+                    const uint32_t e = tid + k * NT;
+                    const double y = spg_reads_out<OP>::value ? told[e] : 0.0;
+                    tout[e] = spg_apply<OP>(tin[tab[k]], y, fac);
+                }
             }
         }
         spg_fence_async_smem();             // generic-proxy writes -> visible to the bulk store

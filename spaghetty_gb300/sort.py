@@ -165,7 +165,9 @@ def plan(dims: Sequence[int], perm: Sequence[int], op: int = 0):
         "perm": [int(info.perm[q]) for q in range(r)],
         "box": [int(info.box[q]) for q in range(r)],
         "threads": info.threads, "ept": info.ept, "ntiles": int(info.ntiles),
-        "run_in": info.run_in, "run_out": info.run_out, "pad": info.pad_period,
+        "run_in": info.run_in, "run_out": info.run_out,
+        "pad": info.pad_period if info.kind != 4 else 0,
+        "skew": info.pad_period if info.kind == 4 else 0,
         "masked": bool(info.masked), "stages": info.stages, "smem_bytes": info.smem_bytes,
     }
 
@@ -175,15 +177,13 @@ __all__ = ["tce_sort_2", "tce_sortacc_2", "tce_sort_4", "tce_sortacc_4", "tce_so
            "plan", "permuted_shape", "SpaghettyError"]
 
 
-def sortacc_fused(out, sources, perms, factors, stream=None):
-    """out += sum_k factors[k] * sources[k].permute(perms[k] - 1), added in k
-    order with the rounding of consecutive tce_sortacc calls, reading and
-    writing ``out`` once (spaghetty_sortacc_fused).  CUDA FP64 tensors; each
-    source has its own shape (the dims a tce_sortacc call would pass)."""
+def _fused(entry, out, sources, perms, factors, stream):
     from ._lib import int_array
     n = len(sources)
     if not (len(perms) == n == len(factors)) or n == 0:
-        raise ValueError("sources, perms and factors must have one entry per sortacc")
+        raise ValueError("sources, perms and factors must have one entry per term")
+    if out.dtype != torch.float64 or not out.is_contiguous() or not out.is_cuda:
+        raise TypeError("the output must be a contiguous CUDA FP64 tensor")
     rank = sources[0].dim()
     dims, pp, ptrs = [], [], []
     for s, p in zip(sources, perms):
@@ -201,7 +201,23 @@ def sortacc_fused(out, sources, perms, factors, stream=None):
         stream = torch.cuda.current_stream(out.device).cuda_stream
     src_arr = (ctypes.c_void_p * n)(*ptrs)
     fac = (ctypes.c_double * n)(*[float(f) for f in factors])
-    rc = lib().spaghetty_sortacc_fused(rank, n, src_arr, int_array(dims), int_array(pp), fac,
-                                       ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(int(stream)))
-    check(rc, "sortacc_fused")
+    rc = getattr(lib(), entry)(rank, n, src_arr, int_array(dims), int_array(pp), fac,
+                               ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(int(stream)))
+    check(rc, entry)
     return out
+
+
+def sortacc_fused(out, sources, perms, factors, stream=None):
+    """out += sum_k factors[k] * sources[k].permute(perms[k] - 1), added in k
+    order with the rounding of consecutive tce_sortacc calls, reading and
+    writing ``out`` once (spaghetty_sortacc_fused).  CUDA FP64 tensors; each
+    source has its own shape (the dims a tce_sortacc call would pass)."""
+    return _fused("spaghetty_sortacc_fused", out, sources, perms, factors, stream)
+
+
+def sort_fused(out, sources, perms, factors, stream=None):
+    """out = sum_k factors[k] * sources[k].permute(perms[k] - 1): the first
+    term as tce_sort computes it, the others added in k order as tce_sortacc
+    does, without reading ``out`` (spaghetty_sort_fused).  Sources may
+    repeat."""
+    return _fused("spaghetty_sort_fused", out, sources, perms, factors, stream)
