@@ -114,6 +114,10 @@ PROTOTYPES = {
                                                ctypes.POINTER(ctypes.c_void_p), c_int_p, c_int_p,
                                                ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
                                                ctypes.c_void_p]),
+    "spaghetty_sort_fused": (ctypes.c_int, [ctypes.c_int, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_void_p), c_int_p, c_int_p,
+                                            ctypes.POINTER(ctypes.c_double), ctypes.c_void_p,
+                                            ctypes.c_void_p]),
     "spaghetty_sort_batch_noalloc": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
     "spaghetty_contract_4x4": (ctypes.c_int, [ctypes.c_void_p, c_int_p, c_int_p, ctypes.c_void_p,
                                               c_int_p, c_int_p, ctypes.c_void_p, c_int_p,

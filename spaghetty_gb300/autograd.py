@@ -1,13 +1,16 @@
 """Differentiable tensor sorts.
 
 ``permute_sum(x, perms, factors)`` computes y = sum_k f_k * permute_k(x)
-as one sort followed by sortaccs, in k order (each term's product rounded,
-then each sum rounded), with the GPU kernels.  Its backward is the adjoint
-of a permutation: dx = sum_k f_k * permute_{p_k^-1}(dy), computed by the
-same kernels as one sort and sortaccs with the inverse permutations -- the
-reference's sortacc (trunk/old_sort.f:512-575) applied to the incoming
-gradient.  ``permute_k`` follows the reference convention: the output holds
-x's index p_q in position q, i.e. ``x.permute(p - 1)`` (1-based p).
+with the rounding of one sort followed by sortaccs, in k order (each term's
+product rounded, then each sum rounded), in ONE fused kernel launch
+(spaghetty_sort_fused: x read once per term, y written once, y never read).
+Its backward is the adjoint of a permutation: dx = sum_k f_k *
+permute_{p_k^-1}(dy) -- the reference's sortacc (trunk/old_sort.f:512-575)
+applied to the incoming gradient -- again one fused launch with the inverse
+permutations.  ``permute_k`` follows the reference convention: the output
+holds x's index p_q in position q, i.e. ``x.permute(p - 1)`` (1-based p).
+Ranks above 6 (or more than 16 terms) run the same arithmetic as one sort
+and sortacc launches.
 """
 from __future__ import annotations
 
@@ -15,7 +18,7 @@ from typing import Sequence
 
 import torch
 
-from .sort import permuted_shape, sort_generic
+from .sort import permuted_shape, sort_fused, sort_generic
 
 
 def inverse(perm: Sequence[int]) -> tuple:
@@ -26,9 +29,12 @@ def inverse(perm: Sequence[int]) -> tuple:
 
 
 def _chain(x: torch.Tensor, perms, factors, out_shape) -> torch.Tensor:
-    """sum_k f_k * permute_k(x) by one sort and len-1 sortaccs."""
+    """sum_k f_k * permute_k(x) with the rounding of one sort and len-1
+    sortaccs: one fused launch where the fused kernels take the rank."""
     y = torch.empty(out_shape, dtype=x.dtype, device=x.device)
     xs = x.contiguous()
+    if xs.dim() <= 6 and len(perms) <= 16:
+        return sort_fused(y, [xs] * len(perms), perms, factors)
     for k, (p, f) in enumerate(zip(perms, factors)):
         sort_generic(xs, y, tuple(xs.shape), p, float(f), 0.0 if k == 0 else 1.0)
     return y
@@ -62,15 +68,3 @@ def permute(x: torch.Tensor, perm: Sequence[int], factor: float = 1.0) -> torch.
     """factor * x.permute(perm - 1) materialised by the GPU kernels,
     differentiable (the backward is the inverse-permutation sort)."""
     return PermuteSum.apply(x, [tuple(perm)], [factor])
-
-
-def reference_grad(dy: torch.Tensor, perms, factors) -> torch.Tensor:
-    """The torch.permute reference gradient built the same way on the CPU:
-    dx = f_1*dy.permute(inv_1), then dx = dx + f_k*dy.permute(inv_k)
-    (separate multiply and add, FP64)."""
-    dyc = dy.detach().cpu()
-    dx = None
-    for p, f in zip(perms, factors):
-        term = torch.mul(dyc.permute([v - 1 for v in inverse(p)]), f)
-        dx = term.contiguous() if dx is None else torch.add(dx, term)
-    return dx

@@ -58,7 +58,8 @@ struct FusedParams {
     int64_t gsrc[SPG_FUSED_MAXS][SPG_FUSED_MAXR];
     const double *src[SPG_FUSED_MAXS];
     SpgFactor fac[SPG_FUSED_MAXS];
-    int32_t op[SPG_FUSED_MAXS];            // OP_ACC_* per source
+    int32_t op[SPG_FUSED_MAXS];            // OP_ACC_* per source (OP_SORT_* for source 0 when first_sets)
+    int32_t first_sets;                    // 1: source 0's product starts the sum, the output is not read
 };
 
 template <int OPA>
@@ -68,6 +69,12 @@ __device__ __forceinline__ double spg_fused_add(double acc, double x, const SpgF
 
 __device__ __forceinline__ double spg_fused_apply(int op, double acc, double x, const SpgFactor &F) {
     switch (op) {
+        // the first term of a fused sort (first_sets): the rounded product
+        // alone, as tce_sort computes it
+        case OP_SORT_ONE: return spg_apply<OP_SORT_ONE>(x, 0.0, F);
+        case OP_SORT_NEG: return spg_apply<OP_SORT_NEG>(x, 0.0, F);
+        case OP_SORT_POW2: return spg_apply<OP_SORT_POW2>(x, 0.0, F);
+        case OP_SORT_ANY: return spg_apply<OP_SORT_ANY>(x, 0.0, F);
         case OP_ACC_ONE: return spg_fused_add<OP_ACC_ONE>(acc, x, F);
         case OP_ACC_NEG: return __dsub_rn(acc, x);   // acc + x*(-1): one rounding
         case OP_ACC_POW2: return spg_fused_add<OP_ACC_POW2>(acc, x, F);
@@ -160,7 +167,7 @@ spg_fused_sortacc(double *__restrict__ out, const __grid_constant__ FusedParams 
         double acc[SPG_FUSED_EPT];
 #pragma unroll
         for (int m = 0; m < SPG_FUSED_EPT; ++m)
-            acc[m] = ooff[m] >= 0 ? spg_ld_out(out + obase + ooff[m]) : 0.0;
+            acc[m] = (ooff[m] >= 0 && !p.first_sets) ? spg_ld_out(out + obase + ooff[m]) : 0.0;
         for (int k = 0; k < p.nsrc; ++k) {
             if (k + 1 < p.nsrc) issue(k + 1, (k + 1) & 1);
             else spg_cp_commit();
@@ -215,6 +222,7 @@ struct FusedTmaParams {
     uint32_t tx_out, tx_src;                       // bytes one load delivers
     SpgFactor fac[SPG_FT_MAXS];
     int32_t op[SPG_FT_MAXS];
+    int32_t first_sets;                            // 1: no old-output item; source 0 starts the sum
     int *status;
 };
 
@@ -253,7 +261,9 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
     const uint32_t free0 = done0 + 16u;
     const uint32_t tid = threadIdx.x;
     const uint32_t G = gridDim.x;
-    const int items = p.nsrc + 1;
+    // items per box: the old output tile (unless first_sets), then the sources
+    const int lead = p.first_sets ? 0 : 1;
+    const int items = p.nsrc + lead;
     const uint32_t load_tid = NT, store_tid = NT + 32;
 
     if (tid == load_tid) {
@@ -307,11 +317,12 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
                     ok = spg_mbar_wait(empty0 + 8u * (uint32_t)s, (uint32_t)(((j / S) - 1) & 1));
                     if (!ok) break;
                 }
+                const int map = i + 1 - lead;       // 0 = output, 1.. = sources
                 int32_t c[5];
-                spg_ft_coords(p, i, t, c);
+                spg_ft_coords(p, map, t, c);
                 const uint32_t mb = full0 + 8u * (uint32_t)s;
-                spg_mbar_expect_tx(mb, i == 0 ? p.tx_out : p.tx_src);
-                spg_tma_load5(base + (uint32_t)s * tb, &maps.m[i], c, mb);
+                spg_mbar_expect_tx(mb, map == 0 ? p.tx_out : p.tx_src);
+                spg_tma_load5(base + (uint32_t)s * tb, &maps.m[map], c, mb);
             }
         }
         if (!ok && p.status) *(volatile int *)p.status = 1;
@@ -347,12 +358,14 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
     bool ok = true;
     for (uint32_t t = blockIdx.x; t < p.ntiles && ok; t += G, ++it) {
         double acc[EPT];
+#pragma unroll
+        for (int m = 0; m < EPT; ++m) acc[m] = 0.0;
         for (int i = 0; i < items; ++i, ++j) {
             const int s = (int)(j % S);
             ok = __all_sync(0xffffffffu, spg_mbar_wait(full0 + 8u * (uint32_t)s, (uint32_t)((j / S) & 1)));
             if (!ok) break;
             const unsigned char *slot = smem + (size_t)s * tb;
-            if (i == 0) {
+            if (i < lead) {
                 const double *told = reinterpret_cast<const double *>(slot);
 #pragma unroll
                 for (int m = 0; m < EPT; ++m) {
@@ -361,9 +374,10 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
                     acc[m] = told[tid + (uint32_t)m * NT];
                 }
             } else {
-                const SpgFactor F = p.fac[i - 1];
-                const int op = p.op[i - 1];
-                const bool rf = p.src_r_first[i - 1] != 0;
+                const int k = i - lead;
+                const SpgFactor F = p.fac[k];
+                const int op = p.op[k];
+                const bool rf = p.src_r_first[k] != 0;
 #pragma unroll
                 for (int m = 0; m < EPT; ++m) {
                     if (soff[m] == 0xFFFFFFFFu) break;
@@ -513,10 +527,10 @@ static bool ft_map(int R, const int *order, const int64_t *ext, const int64_t *s
 static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
                          int nsrc, const double *const *unsorted, const double *factors, double *sorted,
                          void *stream, int p, int q, int r, const int64_t *L, int64_t pw,
-                         FusedTmaParams *PP, FusedTmaMaps *MM, bool launch);
+                         FusedTmaParams *PP, FusedTmaMaps *MM, bool launch, bool first_sets);
 static int fused_tma_mode(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
                           int nsrc, const double *const *unsorted, const double *factors, double *sorted,
-                          void *stream, int p, int q, int64_t lq, int64_t lp, int64_t pw);
+                          void *stream, int p, int q, int64_t lq, int64_t lp, int64_t pw, bool first_sets);
 
 // The TMA-staged pass, or SPAGHETTY_ERR_NOKERNEL when the shapes or the
 // buffers do not allow it (the caller then runs the cp.async kernel).
@@ -524,7 +538,7 @@ static int fused_tma_mode(int R, const int64_t *O, const int64_t *ostr, int64_t 
 // sstr[k]: each kept dim's element stride in source k.
 static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
                           int nsrc, const double *const *unsorted, const double *factors, double *sorted,
-                          void *stream) {
+                          void *stream, bool first_sets) {
     if (R < 2 || nsrc < 1 || nsrc > SPG_FT_MAXS) return SPAGHETTY_ERR_NOKERNEL;
     if (((uintptr_t)sorted & 15u) != 0) return SPAGHETTY_ERR_NOKERNEL;
     for (int k = 0; k < nsrc; ++k)
@@ -554,7 +568,7 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
             if ((pw / 2) % 2 == 0) pw += 2;
         }
         const int rc = fused_tma_mode(R, O, ostr, sstr, nsrc, unsorted, factors, sorted, stream, p, q, lq,
-                                      lp, pw);
+                                      lp, pw, first_sets);
         if (rc != SPAGHETTY_ERR_NOKERNEL) return rc;
     }
     return SPAGHETTY_ERR_NOKERNEL;
@@ -565,7 +579,7 @@ static int fused_tma_pass(int R, const int64_t *O, const int64_t *ostr, int64_t 
 // maps fit, then the launch.
 static int fused_tma_mode(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
                           int nsrc, const double *const *unsorted, const double *factors, double *sorted,
-                          void *stream, int p, int q, int64_t lq, int64_t lp, int64_t pw) {
+                          void *stream, int p, int q, int64_t lq, int64_t lp, int64_t pw, bool first_sets) {
     static thread_local FusedTmaParams P;
     static thread_local FusedTmaMaps M;
     // the third box dim r: the one giving the largest box whose maps stay
@@ -586,7 +600,7 @@ static int fused_tma_mode(int R, const int64_t *O, const int64_t *ostr, int64_t 
         const int64_t vol = lp * lq * (r >= 0 ? L[r] : 1);
         if (vol <= best_vol) continue;
         if (fused_tma_try(R, O, ostr, sstr, nsrc, unsorted, factors, sorted, stream, p, q, r < 0 ? p : r, L,
-                          pw, &P, &M, false) != SPAGHETTY_OK)
+                          pw, &P, &M, false, first_sets) != SPAGHETTY_OK)
             continue;
         best_r = r;
         best_vol = vol;
@@ -594,7 +608,7 @@ static int fused_tma_mode(int R, const int64_t *O, const int64_t *ostr, int64_t 
     }
     if (best_r == -2) return SPAGHETTY_ERR_NOKERNEL;
     return fused_tma_try(R, O, ostr, sstr, nsrc, unsorted, factors, sorted, stream, p, q,
-                         best_r < 0 ? p : best_r, bestL, pw, &P, &M, true);
+                         best_r < 0 ? p : best_r, bestL, pw, &P, &M, true, first_sets);
 }
 
 // One attempt at the TMA-staged pass with box L (16 along p, lq along q,
@@ -602,7 +616,7 @@ static int fused_tma_mode(int R, const int64_t *O, const int64_t *ostr, int64_t 
 static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (*sstr)[SPG_FUSED_MAXR],
                          int nsrc, const double *const *unsorted, const double *factors, double *sorted,
                          void *stream, int p, int q, int r, const int64_t *L, int64_t pw,
-                         FusedTmaParams *PP, FusedTmaMaps *MM, bool launch) {
+                         FusedTmaParams *PP, FusedTmaMaps *MM, bool launch, bool first_sets) {
     FusedTmaParams &P = *PP;
     FusedTmaMaps &M = *MM;
     const int64_t lq = L[q], lr = r == p ? 1 : L[r], lp = L[p];
@@ -668,9 +682,11 @@ static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (
     P.tx_out = (uint32_t)(vol * 8);
     P.tx_src = (uint32_t)(vol_src * 8);
     for (int k = 0; k < nsrc; ++k) {
-        P.fac[k] = spg_make_factor(factors[k], 1.0);
-        P.op[k] = spg_choose_op(factors[k], 1.0);
+        const double g = (first_sets && k == 0) ? 0.0 : 1.0;
+        P.fac[k] = spg_make_factor(factors[k], g);
+        P.op[k] = spg_choose_op(factors[k], g);
     }
+    P.first_sets = first_sets ? 1 : 0;
     P.status = spg_status_word();
     if (!launch) return SPAGHETTY_OK;
     const size_t smem = (size_t)(SPG_FT_S + 2) * P.tile_bytes + (2 * SPG_FT_S + 4) * 8 + 1024;
@@ -696,7 +712,8 @@ static int fused_tma_try(int R, const int64_t *O, const int64_t *ostr, int64_t (
 }
 
 static int fused_pass(int rank, int nsrc, const double *const *unsorted, const int *dims,
-                      const int *perms, const double *factors, double *sorted, void *stream) {
+                      const int *perms, const double *factors, double *sorted, void *stream,
+                      bool first_sets, bool allow_tma) {
     if (rank < 1 || rank > SPG_FUSED_MAXR) return SPAGHETTY_ERR_RANK;
     if (nsrc < 1 || nsrc > SPG_FUSED_MAXS) return SPAGHETTY_ERR_CONFIG;
     if (!unsorted || !dims || !perms || !factors) return SPAGHETTY_ERR_NULL;
@@ -747,8 +764,8 @@ static int fused_pass(int rank, int nsrc, const double *const *unsorted, const i
     }
     int64_t ostr[SPG_FUSED_MAXR];
     for (int i = 0; i < R; ++i) ostr[i] = ostride_full[keep[i]];
-    {
-        const int rc = fused_tma_pass(R, O, ostr, sstride, nsrc, unsorted, factors, sorted, stream);
+    if (allow_tma) {
+        const int rc = fused_tma_pass(R, O, ostr, sstride, nsrc, unsorted, factors, sorted, stream, first_sets);
         if (rc != SPAGHETTY_ERR_NOKERNEL) return rc;
     }
     // layouts: 0 = output, 1.. = sources; each lists the kept dims fastest first
@@ -795,10 +812,11 @@ static int fused_pass(int rank, int nsrc, const double *const *unsorted, const i
         }
         if (smax > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
         P.src[k] = unsorted[k];
-        const double g = 1.0;
+        const double g = (first_sets && k == 0) ? 0.0 : 1.0;
         P.fac[k] = spg_make_factor(factors[k], g);
         P.op[k] = spg_choose_op(factors[k], g);
     }
+    P.first_sets = first_sets ? 1 : 0;
     if (maxoff > INT32_MAX) return SPAGHETTY_ERR_NOKERNEL;
     // pad: one slot every `pad` canonical elements, picked to spread the
     // scattered source writes over the banks (fewest simulated conflicts)
@@ -877,10 +895,17 @@ static int fused_pass(int rank, int nsrc, const double *const *unsorted, const i
 // their stride-1 index: one box then gives every source and the output
 // long contiguous runs.  The nine triples sortaccs of one group touch one to
 // three such indices, i.e. one to three passes over t3 instead of nine.
-extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *unsorted,
-                                       const int *dims, const int *perms, const double *factors,
-                                       double *sorted, void *stream) {
-    SpgRange range("spaghetty_sortacc_fused");
+// Outputs of at most SPG_FUSED_ONE_PASS elements (L2-resident, where a
+// launch costs more than the shorter runs) take all the sources in one pass
+// of the cp.async kernel instead.  first_sets: the first source's product
+// starts the sum (a sort followed by sortaccs); the first pass then does not
+// read the output.
+#define SPG_FUSED_ONE_PASS (int64_t(1) << 22)
+
+static int fused_entry(const char *name, int rank, int nsrc, const double *const *unsorted,
+                       const int *dims, const int *perms, const double *factors, double *sorted,
+                       void *stream, bool first_sets) {
+    SpgRange range(name);
     if (rank < 1 || rank > SPG_FUSED_MAXR) return SPAGHETTY_ERR_RANK;
     if (nsrc < 1 || nsrc > SPG_FUSED_MAXS) return SPAGHETTY_ERR_CONFIG;
     if (!unsorted || !dims || !perms || !factors) return SPAGHETTY_ERR_NULL;
@@ -899,11 +924,9 @@ extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *
                 if (perms[k * rank + q] == i + 1) fast[k] = q;
         }
     }
-    {
-        int64_t n0 = 1;
-        for (int q = 0; q < rank; ++q) n0 *= dims[q] > 0 ? dims[q] : 0;
-        if (n0 == 0) return SPAGHETTY_OK;   // empty tensors: nothing to do
-    }
+    int64_t n0 = 1;
+    for (int q = 0; q < rank; ++q) n0 *= dims[q] > 0 ? dims[q] : 0;
+    if (n0 == 0) return SPAGHETTY_OK;   // empty tensors: nothing to do
     // device (or managed) memory of one device only: the kernel reads and
     // writes these pointers directly; the work runs on that device
     int dev = -1;
@@ -926,15 +949,34 @@ extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *
         cudaGetLastError();
         return SPAGHETTY_ERR_CUDA;
     }
+    int passes = 1;
+    for (int k = 1; k < nsrc; ++k) passes += fast[k] != fast[k - 1];
     int rc = SPAGHETTY_OK;
-    int k0 = 0;
-    while (k0 < nsrc && rc == SPAGHETTY_OK) {
-        int k1 = k0 + 1;
-        while (k1 < nsrc && fast[k1] == fast[k0]) ++k1;
-        rc = fused_pass(rank, k1 - k0, unsorted + k0, dims + k0 * rank, perms + k0 * rank,
-                        factors + k0, sorted, stream);
-        k0 = k1;
+    if (passes > 1 && n0 <= SPG_FUSED_ONE_PASS) {
+        rc = fused_pass(rank, nsrc, unsorted, dims, perms, factors, sorted, stream, first_sets, false);
+    } else {
+        int k0 = 0;
+        while (k0 < nsrc && rc == SPAGHETTY_OK) {
+            int k1 = k0 + 1;
+            while (k1 < nsrc && fast[k1] == fast[k0]) ++k1;
+            rc = fused_pass(rank, k1 - k0, unsorted + k0, dims + k0 * rank, perms + k0 * rank,
+                            factors + k0, sorted, stream, first_sets && k0 == 0, true);
+            k0 = k1;
+        }
     }
     if (cur >= 0 && cur != dev) cudaSetDevice(cur);
     return rc;
+}
+
+extern "C" int spaghetty_sortacc_fused(int rank, int nsrc, const double *const *unsorted,
+                                       const int *dims, const int *perms, const double *factors,
+                                       double *sorted, void *stream) {
+    return fused_entry("spaghetty_sortacc_fused", rank, nsrc, unsorted, dims, perms, factors, sorted,
+                       stream, false);
+}
+
+extern "C" int spaghetty_sort_fused(int rank, int nsrc, const double *const *unsorted, const int *dims,
+                                    const int *perms, const double *factors, double *sorted, void *stream) {
+    return fused_entry("spaghetty_sort_fused", rank, nsrc, unsorted, dims, perms, factors, sorted, stream,
+                       true);
 }

@@ -12,6 +12,25 @@ pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
 
 
+def inverse(perm):
+    inv = [0] * len(perm)
+    for q, p in enumerate(perm):
+        inv[p - 1] = q + 1
+    return tuple(inv)
+
+
+def reference_grad(dy, perms, factors):
+    """The torch.permute reference gradient built the same way on the CPU:
+    dx = f_1*dy.permute(inv_1), then dx = dx + f_k*dy.permute(inv_k)
+    (separate multiply and add, FP64)."""
+    dyc = dy.detach().cpu()
+    dx = None
+    for p, f in zip(perms, factors):
+        term = torch.mul(dyc.permute([v - 1 for v in inverse(p)]), f)
+        dx = term.contiguous() if dx is None else torch.add(dx, term)
+    return dx
+
+
 def seeded_perms(r, seed):
     rnd = random.Random(seed)
     out = []
@@ -25,7 +44,7 @@ def seeded_perms(r, seed):
 
 @pytest.mark.parametrize("dims", [(24, 24, 24, 24), (12, 12, 12, 12, 12, 12)])
 def test_backward_bit_exact_and_finite_differences(cuda, dims):
-    from spaghetty_gb300.autograd import permute_sum, reference_grad
+    from spaghetty_gb300.autograd import permute_sum
     r = len(dims)
     perms = seeded_perms(r, 17 + r)
     factors = (0.75, -1.25, 0.3)
@@ -73,7 +92,7 @@ def test_backward_bit_exact_and_finite_differences(cuda, dims):
 def test_backward_on_autograd_thread_bench_perms(cuda):
     """The benchmark's perms at 24^4 (4321 runs on the TMA-staged kernel);
     the backward runs on the autograd engine's own worker thread."""
-    from spaghetty_gb300.autograd import permute_sum, reference_grad
+    from spaghetty_gb300.autograd import permute_sum
     dims = (24, 24, 24, 24)
     perms = [(4, 3, 2, 1), (2, 4, 1, 3), (3, 1, 4, 2)]
     factors = (0.75, -1.25, 0.3)

@@ -77,3 +77,51 @@ def test_triples_partial_boxes(cuda, group):
     factors = [rnd.choice([1.0, -1.0, 0.5]) for _ in perms]
     run_group(cuda, (20, 12, 18, 20, 12, 18), perms, factors, 900 + group)
     run_group(cuda, (18, 6, 20, 18, 6, 19), perms, factors, 950 + group)
+
+
+def run_sort_group(cuda, out_shape, perms, factors, seed, same_source=False):
+    """spaghetty_sort_fused: the first term overwrites (as tce_sort), the
+    rest accumulate (as tce_sortacc); the output starts as NaN garbage,
+    which must never be read, and the first source holds signed zeros."""
+    from spaghetty_gb300 import sort_fused
+    n = int(np.prod(out_shape))
+    srcs_h = []
+    for k, p in enumerate(perms):
+        if same_source and k > 0:
+            srcs_h.append(srcs_h[0])
+            continue
+        x = O.fixture_values(n, seed + 100 + k)
+        if k == 0:
+            x[::7] = -0.0
+        srcs_h.append(x)
+    want = O.np_sort(srcs_h[0], source_shape(out_shape, perms[0]), perms[0], factors[0], 0.0)
+    for x, p, f in zip(srcs_h[1:], perms[1:], factors[1:]):
+        want = O.np_sort(x, source_shape(out_shape, p), p, f, 1.0, out=want)
+    dsrc = [torch.from_numpy(x).to(cuda).reshape(source_shape(out_shape, p))
+            for x, p in zip(srcs_h, perms)]
+    dout = torch.full(out_shape, float("nan"), dtype=torch.float64, device=cuda)
+    sort_fused(dout, dsrc, perms, factors)
+    got = dout.cpu().numpy().reshape(-1)
+    assert bits_equal(got, want), (out_shape, first_mismatch(got, want))
+
+
+@pytest.mark.parametrize("group", [0, 1, 2])
+def test_sort_fused_first_term_overwrites(cuda, group):
+    perms = TRIPLES_SORTACC6[group]
+    rnd = random.Random(60 + group)
+    factors = [1.0] + [rnd.choice([1.0, -1.0, 0.5, -0.3]) for _ in perms[1:]]
+    run_sort_group(cuda, (8, 10, 6, 8, 10, 6), perms, factors, 70 * group)
+    run_sort_group(cuda, (16, 16, 16, 16, 16, 16), perms, factors, 70 * group + 5)
+    # a lone term is a plain sort (signed zeros kept)
+    run_sort_group(cuda, (8, 10, 6, 8, 10, 6), perms[:1], [1.0], 70 * group + 9)
+
+
+@pytest.mark.parametrize("shape", [(24, 24, 24, 24), (12, 12, 12, 12, 12, 12), (46, 46, 46, 46)])
+def test_sort_fused_repeated_source(cuda, shape):
+    """The differentiable sort's pattern: one source under several perms
+    whose stride-1 indices differ (one cp.async pass for L2-sized outputs,
+    TMA passes above 2^22 elements)."""
+    r = len(shape)
+    perms = [tuple(range(r, 0, -1)), tuple([2, 1] + list(range(3, r + 1))),
+             tuple(list(range(2, r + 1)) + [1])]
+    run_sort_group(cuda, shape, perms, [0.75, -1.25, 0.3], 31 + r, same_source=True)
