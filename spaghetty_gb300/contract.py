@@ -10,11 +10,12 @@ from __future__ import annotations
 import ctypes
 from typing import Sequence
 
+import numpy as np
 import torch
 
 from ._lib import check, int_array, lib
 
-MODES = {"exact": 0, "fma": 1}
+MODES = {"exact": 0, "fma": 1, "mma": 2}
 
 
 def contract_shapes(dims_a: Sequence[int], perm_a: Sequence[int], dims_b: Sequence[int],
@@ -33,7 +34,8 @@ def contract_4x4(a, dims_a, perm_a, b, dims_b, perm_b, c, perm_c, alpha=1.0, fac
     """c (=|+=) factor * sort_{perm_c}( sort_{perm_a}(a)[M,K] x sort_{perm_b}(b)[N,K]^T )
     on CUDA FP64 tensors, queued on torch's current stream (or ``stream``).
     ``mode`` "exact" adds the products in k order with every product and sum
-    rounded (the skeleton's loop_dgemm bits); "fma" uses fused multiply-adds."""
+    rounded (the skeleton's loop_dgemm bits); "fma" uses fused multiply-adds;
+    "mma" FP64 matrix instructions (mma.sync .f64)."""
     _, _, _, dims_c = contract_shapes(dims_a, perm_a, dims_b, perm_b, perm_c)
     for t in (a, b, c):
         if t.dtype != torch.float64 or not t.is_cuda or not t.is_contiguous():
@@ -62,6 +64,13 @@ def ccsd_t2_8(a_raw, b_raw, c_done, dims: Sequence[int]):
     d1, d2, d3, d4, d5, d6 = (int(x) for x in dims)
     for t, need, name in ((a_raw, d5 * d6 * d1 * d2, "a_raw"), (b_raw, d3 * d4 * d5 * d6, "b_raw"),
                           (c_done, d1 * d2 * d3 * d4, "c_done")):
+        # the C drop-in reads and writes 8 bytes per element from the start
+        # of each buffer: anything but contiguous FP64 would run past its end
+        if isinstance(t, torch.Tensor):
+            if t.dtype != torch.float64 or not t.is_contiguous():
+                raise TypeError("%s must be a contiguous FP64 tensor" % name)
+        elif getattr(t, "dtype", None) != np.float64 or not t.flags.c_contiguous:
+            raise TypeError("%s must be a C-contiguous float64 array" % name)
         n = t.numel() if isinstance(t, torch.Tensor) else t.size
         if n < need:
             raise ValueError("%s has %d elements, the dims need %d" % (name, n, need))

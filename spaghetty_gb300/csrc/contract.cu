@@ -22,7 +22,12 @@
 //               and sum rounded -- the bits of loop_dgemm case 3 on a zeroed
 //               c_sort (alpha*a rounded first, as Fortran evaluates it);
 //   fma mode:   the same order with a fused multiply-add per term (faster,
-//               not bit-identical to the loop).
+//               not bit-identical to the loop);
+//   mma mode:   FP64 matrix instructions (spg_contract_mma below), within
+//               rounding of the loop like fma mode.
+// Exact mode cannot use a matrix instruction: the loop's bits need every
+// product rounded, then added to the running sum in k order, while an MMA
+// fuses each product into a sum of several terms.
 // The result goes through the sorts' factor arithmetic: c_done = f*s (sort)
 // or c_done + f*s (sortacc), exactly as tce_sort_4 / tce_sortacc_4 of c_sort.
 //
@@ -178,9 +183,141 @@ spg_contract(const __grid_constant__ ContractParams p) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// mma mode: the same fused sort -> GEMM -> sort with the products summed by
+// FP64 matrix instructions (mma.sync m8n8k4, .f64): one instruction per warp
+// multiplies an 8x4 slice of A by a 4x8 slice of B into an 8x8 accumulator.
+// A CTA of four warps owns a 16x16 output tile; each staged block of 32
+// contracted indices is split over the warps (warp w takes the 4-wide steps
+// w, w+4, ...), every warp accumulating the whole tile (four 8x8
+// sub-tiles), and the four partial tiles are added at the end.  Like fma
+// mode it is within rounding of the loop, not bit-identical (the order of
+// the additions differs).  Fragment layouts of m8n8k4 .f64 (PTX ISA): a0 =
+// A[lane/4][lane%4], b0 = B[lane%4][lane/4], d = D[lane/4][2*(lane%4)+i].
+// The staging rows are padded to 20 doubles: a half warp's fragment reads
+// (4 k rows x 4 consecutive m) then fall in 16 different bank pairs.
+#define SPG_CTM_NT 128
+#define SPG_CTM_PITCH 20
+
+__device__ __forceinline__ void spg_dmma(double &d0, double &d1, double a, double b) {
+    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};\n"
+                 : "+d"(d0), "+d"(d1)
+                 : "d"(a), "d"(b));
+}
+
+template <int OP>
+__global__ void __launch_bounds__(SPG_CTM_NT)
+spg_contract_mma(const __grid_constant__ ContractParams p) {
+    constexpr int KROWS = SPG_CTM_NT / 16;          // k rows one staging pass covers
+    constexpr int LPT = SPG_CT_TK / KROWS;          // staged elements per thread and operand
+    __shared__ __align__(16) double As[2][SPG_CT_TK][SPG_CTM_PITCH];
+    __shared__ __align__(16) double Bs[2][SPG_CT_TK][SPG_CTM_PITCH];
+    __shared__ double part[4][SPG_CT_TM][SPG_CT_TN];   // per-warp partial tiles
+    const uint32_t tid = threadIdx.x;
+    const uint32_t lane = tid & 31u, warp = tid >> 5;
+    const uint32_t g = lane >> 2, t4 = lane & 3u;
+    const uint32_t lrow = tid & 15u, lk = tid >> 4;
+    const SpgFactor fac = p.fac;
+    for (uint32_t t = blockIdx.x; t < p.ntiles; t += gridDim.x) {
+        const uint32_t tn = fd_div(t, p.mtiles);
+        const uint32_t tm = t - tn * p.mtiles.d;
+        const uint32_t m0 = tm * SPG_CT_TM, n0 = tn * SPG_CT_TN;
+        const bool lm_ok = m0 + lrow < (uint32_t)p.M, ln_ok = n0 + lrow < (uint32_t)p.N;
+        const int64_t offa = lm_ok ? spg_g2(p.am, m0 + lrow) : 0;
+        const int64_t offb = ln_ok ? spg_g2(p.bn, n0 + lrow) : 0;
+        auto fetch = [&](int32_t k0, int buf) {
+#pragma unroll
+            for (int j = 0; j < LPT; ++j) {
+                const uint32_t kk = lk + (uint32_t)KROWS * j;
+                const uint32_t k = (uint32_t)k0 + kk;
+                const bool kin = k < (uint32_t)p.K;
+                const bool a_ok = kin && lm_ok, b_ok = kin && ln_ok;
+                spg_cp_async8((uint32_t)__cvta_generic_to_shared(&As[buf][kk][lrow]),
+                              a_ok ? p.a + offa + spg_g2(p.ak, k) : p.a, a_ok ? 8u : 0u);
+                spg_cp_async8((uint32_t)__cvta_generic_to_shared(&Bs[buf][kk][lrow]),
+                              b_ok ? p.b + offb + spg_g2(p.bk, k) : p.b, b_ok ? 8u : 0u);
+            }
+            spg_cp_commit();
+        };
+        auto scale = [&](int buf) {
+            if (!p.scale_a) return;
+#pragma unroll
+            for (int j = 0; j < LPT; ++j) {
+                double *q = &As[buf][lk + (uint32_t)KROWS * j][lrow];
+                *q = __dmul_rn(p.alpha, *q);
+            }
+        };
+        // acc[i][j][0..1]: sub-tile (8i.., 8j..), elements (g, 2*t4 + 0..1)
+        double acc[2][2][2];
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) acc[i][j][0] = acc[i][j][1] = 0.0;
+        __syncthreads();                    // the previous tile's partials are consumed
+        fetch(0, 0);
+        int buf = 0;
+        for (int32_t k0 = 0; k0 < p.K; k0 += SPG_CT_TK, buf ^= 1) {
+            if (k0 + SPG_CT_TK < p.K) {
+                fetch(k0 + SPG_CT_TK, buf ^ 1);
+                spg_cp_wait<1>();
+            } else {
+                spg_cp_wait<0>();
+            }
+            scale(buf);
+            __syncthreads();
+            // indices past K were zero-filled: whole 4-wide steps are safe
+#pragma unroll
+            for (int s = 0; s < SPG_CT_TK / 16; ++s) {
+                const uint32_t kk = 4u * (warp + 4u * (uint32_t)s) + t4;
+                const double a0 = As[buf][kk][g], a1 = As[buf][kk][8 + g];
+                const double b0 = Bs[buf][kk][g], b1 = Bs[buf][kk][8 + g];
+                spg_dmma(acc[0][0][0], acc[0][0][1], a0, b0);
+                spg_dmma(acc[0][1][0], acc[0][1][1], a0, b1);
+                spg_dmma(acc[1][0][0], acc[1][0][1], a1, b0);
+                spg_dmma(acc[1][1][0], acc[1][1][1], a1, b1);
+            }
+            __syncthreads();                // buffer buf is refilled two steps on
+        }
+        // the four warps' partial tiles, added in warp order
+#pragma unroll
+        for (int i = 0; i < 2; ++i)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+                part[warp][8 * i + g][8 * j + 2 * t4] = acc[i][j][0];
+                part[warp][8 * i + g][8 * j + 2 * t4 + 1] = acc[i][j][1];
+            }
+        __syncthreads();
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const uint32_t idx = tid + (uint32_t)e * SPG_CTM_NT;
+            const uint32_t mi = idx >> 4, ni = idx & 15u;
+            const uint32_t m = m0 + mi, n = n0 + ni;
+            if (m >= (uint32_t)p.M || n >= (uint32_t)p.N) continue;
+            const double s = ((part[0][mi][ni] + part[1][mi][ni]) + part[2][mi][ni]) + part[3][mi][ni];
+            double *dst = p.c + spg_g2(p.cm, m) + spg_g2(p.cn, n);
+            const double y = spg_reads_out<OP>::value ? *dst : 0.0;
+            *dst = spg_apply<OP>(s, y, fac);
+        }
+    }
+}
+
 namespace {
 
 typedef void (*ContractFn)(ContractParams);
+
+ContractFn contract_mma_kernel(int op) {
+    switch (op) {
+        case OP_SORT_ONE: return spg_contract_mma<OP_SORT_ONE>;
+        case OP_SORT_NEG: return spg_contract_mma<OP_SORT_NEG>;
+        case OP_SORT_POW2: return spg_contract_mma<OP_SORT_POW2>;
+        case OP_SORT_ANY: return spg_contract_mma<OP_SORT_ANY>;
+        case OP_ACC_ONE: return spg_contract_mma<OP_ACC_ONE>;
+        case OP_ACC_NEG: return spg_contract_mma<OP_ACC_NEG>;
+        case OP_ACC_POW2: return spg_contract_mma<OP_ACC_POW2>;
+        case OP_ACC_ANY: return spg_contract_mma<OP_ACC_ANY>;
+        default: return spg_contract_mma<OP_GEN>;
+    }
+}
 
 template <bool FMA, int RM, int RN>
 ContractFn contract_kernel(int op) {
@@ -301,7 +438,8 @@ int launch_contract(ContractParams &P, int mode, double factor, double acc_facto
     int dev = 0, sms = 152, nb = 0, nt = 64;
     if (cudaGetDevice(&dev) != cudaSuccess) { cudaGetLastError(); return SPAGHETTY_ERR_CUDA; }
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 152;
-    const ContractFn fn = pick_kernel(op, mode != 0, P.ntiles, sms, &nt);
+    const ContractFn fn = mode == 2 ? contract_mma_kernel(op) : pick_kernel(op, mode != 0, P.ntiles, sms, &nt);
+    if (mode == 2) nt = SPG_CTM_NT;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, (const void *)fn, nt, 0) != cudaSuccess || nb < 1)
         nb = 1;
     cudaGetLastError();
@@ -516,7 +654,7 @@ int spaghetty_contract_4x4(const double *a, const int *dims_a, const int *perm_a
                            const int *dims_b, const int *perm_b, double *c, const int *perm_c,
                            double alpha, double factor, double acc_factor, int mode, void *stream) {
     SpgRange range("spaghetty_contract_4x4");
-    if (mode != 0 && mode != 1) return crecord(SPAGHETTY_ERR_CONFIG);
+    if (mode < 0 || mode > 2) return crecord(SPAGHETTY_ERR_CONFIG);
     ContractParams P;
     memset(&P, 0, sizeof(P));
     int64_t na, nb, nc;

@@ -185,3 +185,19 @@ def test_python_wrappers_check_buffer_sizes():
         contract_4x4(torch.zeros(16, dtype=torch.float64), (2, 2, 2, 2), (1, 2, 3, 4),
                      torch.zeros(24, dtype=torch.float64), (2, 2, 3, 2), (1, 2, 3, 4),
                      torch.zeros(16, dtype=torch.float64), (1, 2, 3, 4))
+
+
+def test_ccsd_t2_8_wrapper_checks_dtype_and_layout():
+    """The drop-in reads 8 bytes per element from each buffer's start: the
+    wrapper refuses other dtypes and strided arrays before any call."""
+    import torch
+
+    from spaghetty_gb300.contract import ccsd_t2_8
+    with pytest.raises(TypeError):
+        ccsd_t2_8(np.zeros(16, dtype=np.float32), np.zeros(16), np.zeros(16), (2,) * 6)
+    with pytest.raises(TypeError):
+        ccsd_t2_8(np.zeros(16), np.zeros(32)[::2], np.zeros(16), (2,) * 6)
+    with pytest.raises(TypeError):
+        ccsd_t2_8(np.zeros(16), np.zeros(16), torch.zeros(16, dtype=torch.float32), (2,) * 6)
+    with pytest.raises(TypeError):
+        ccsd_t2_8(np.zeros(16), np.zeros(16), torch.zeros(32, dtype=torch.float64)[::2], (2,) * 6)

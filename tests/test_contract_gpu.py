@@ -100,9 +100,11 @@ def test_contract_4x4_random_perms_every_factor_bits(cuda, seed):
                                                            first_mismatch(got, want))
 
 
-def test_contract_fma_mode_within_rounding(cuda):
-    """fma mode: the same sums with fused multiply-adds, within K roundings
-    of the exact mode's result (relative to the sum of |products|)."""
+@pytest.mark.parametrize("mode", ["fma", "mma"])
+def test_contract_fma_mode_within_rounding(cuda, mode):
+    """fma mode (fused multiply-adds) and mma mode (FP64 matrix
+    instructions): the same sums within K roundings of the exact mode's
+    result (relative to the sum of |products|)."""
     from spaghetty_gb300.contract import contract_4x4, contract_shapes
     rng = np.random.default_rng(7)
     # sorted operands (20, 24 | 16, 18) and (20, 22 | 16, 18): M 480, N 440, K 288
@@ -116,7 +118,7 @@ def test_contract_fma_mode_within_rounding(cuda):
     bound = O.contract_4x4(np.abs(a), da, pa, np.abs(b), db, pb, pc)
     ga, gb = torch.from_numpy(a).to(cuda), torch.from_numpy(b).to(cuda)
     gc = torch.empty(int(np.prod(dc)), dtype=torch.float64, device=cuda)
-    contract_4x4(ga, da, pa, gb, db, pb, gc, pc, mode="fma")
+    contract_4x4(ga, da, pa, gb, db, pb, gc, pc, mode=mode)
     got = gc.cpu().numpy()
     tol = 2 * K * np.finfo(np.float64).eps * bound
     assert np.all(np.abs(got - want) <= tol)
@@ -124,15 +126,15 @@ def test_contract_fma_mode_within_rounding(cuda):
 
 
 def test_contract_integer_fill_both_modes_exact(cuda):
-    """The skeleton's number_array fill (integer values, exact sums): both
-    modes give exactly the integer result."""
+    """The skeleton's number_array fill (integer values, exact sums): every
+    mode gives exactly the integer result."""
     from spaghetty_gb300.contract import contract_4x4
     d1, d2, d3, d4, d5, d6 = 8, 9, 4, 5, 6, 7
     t = np.arange(1, d5 * d6 * d1 * d2 + 1, dtype=np.float64)
     v = np.arange(1, d3 * d4 * d5 * d6 + 1, dtype=np.float64)
     want = t2_8_oracle(t, v, (d1, d2, d3, d4, d5, d6))
     gt, gv = torch.from_numpy(t).to(cuda), torch.from_numpy(v).to(cuda)
-    for mode in ("exact", "fma"):
+    for mode in ("exact", "fma", "mma"):
         gc = torch.empty(want.size, dtype=torch.float64, device=cuda)
         contract_4x4(gt, (d5, d6, d1, d2), (4, 3, 2, 1), gv, (d3, d4, d5, d6), (2, 1, 4, 3), gc,
                      (2, 1, 4, 3), mode=mode)
@@ -155,7 +157,7 @@ def test_contract_argument_errors(cuda):
     assert call(p(a), p(b), p(c), dims_b=int_array((4, 4, 4, 5))) == 3    # contracted dims differ
     assert call(p(a), p(b), p(c), perm_a=int_array((1, 1, 3, 4))) == 2   # not a permutation
     assert call(p(a), p(b), p(a)) == 6                                    # result overlaps a
-    assert call(p(a), p(b), p(c), mode=2) == 9                            # unknown mode
+    assert call(p(a), p(b), p(c), mode=3) == 9                            # unknown mode
     host = np.zeros(256)
     assert call(p(a), p(b), ctypes.c_void_p(host.ctypes.data)) == 8       # host memory, async form
     assert L.spaghetty_contract_last_error() == 8
