@@ -535,11 +535,12 @@ int spaghetty_batch_destroy(spaghetty_batch *b) {
 // ===========================================================================
 // Batched sorts without any allocation.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
-// being captured (cudaMalloc is illegal there), code that lives inside a
-// host application that owns the device memory budget (a fixed arena
-// handed out by its own allocator), or a tight loop that must not touch the
-// allocator at all.  spaghetty_sort_batch_noalloc() runs the same persistent
+// Some callers cannot call cudaMalloc: an application that has handed the
+// whole device memory to its own pool allocator at start-up (a library's
+// cudaMalloc then fails, or escapes the application's accounting), and code
+// that must not trigger the device-wide synchronisation that cudaMalloc and
+// cudaFree may cause while other streams are running.
+// spaghetty_sort_batch_noalloc() runs the same persistent
 // batched kernel as spaghetty_batch_create()/spaghetty_batch_launch(), but
 // its work list, unit counter and status word live in the file-scope device
 // array below, which every GPU that loads this library holds until exit.
@@ -569,6 +570,9 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
                                             void *stream) {
     if (n < 0 || (n > 0 && !entries)) return SPAGHETTY_ERR_NULL;
     if (n > SPG_NOALLOC_MAX_SORTS) return SPAGHETTY_ERR_TOO_LARGE;
+    // the shipped size-bucket rules, as spaghetty_batch_create loads them,
+    // so that plans do not depend on which batched entry ran first
+    spg_autoload_tune();
     std::lock_guard<std::mutex> lk(g_na_mu);
     g_batch_bad_index = -1;
     int dev = 0;

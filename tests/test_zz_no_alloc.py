@@ -1,22 +1,33 @@
 """The no-allocation batched entry point, spaghetty_sort_batch_noalloc.
 
-It is meant for callers that cannot allocate device memory (code running
-while a CUDA graph is being captured, or inside an application that owns the
-device memory budget): its work list lives in a fixed device array inside the
-library.  Checked here through the C ABI against the allocating batched entry
-point (spaghetty_batch_create + spaghetty_batch_launch) on two calls in a
-row with different sorts, bit for bit -- the tolerance of every parity test
-in this suite -- so a stale work list left in the shared array by the first
-call would show up in the second.  This file is collected last on purpose.
+Some callers cannot allocate device memory: an application that has handed
+the whole device memory to its own pool allocator, or code that must not
+cause the device-wide synchronisation cudaMalloc/cudaFree may trigger while
+other streams run.  This entry point keeps its work list in a fixed device
+array inside the library instead.  Checked here through the C ABI on two
+calls in a row with different sorts, so that a stale work list left in the
+shared array by the first call would show up in the second: bit for bit (the
+tolerance of every parity test in this suite) against the allocating batched
+entry point (spaghetty_batch_create + spaghetty_batch_launch) and against the
+oracle.  One test runs the entry point as the first library call of a fresh
+process, where it does its per-device set-up.  This file is collected last on
+purpose.
 """
 import ctypes
+import os
 import random
+import subprocess
+import sys
 
 import numpy as np
 import pytest
 
+from oracle import oracle as O
+
 pytestmark = pytest.mark.gpu
 torch = pytest.importorskip("torch")
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _specs(seed, n):
@@ -49,21 +60,32 @@ def _entries(specs, ins, outs):
     return arr
 
 
+def _inputs(cuda, specs, seed):
+    gen = torch.Generator(device=cuda)
+    gen.manual_seed(seed)
+    ins, olds = [], []
+    for dims, _, _, _ in specs:
+        k = int(np.prod(dims))
+        ins.append(torch.rand(k, dtype=torch.float64, device=cuda, generator=gen) - 0.5)
+        olds.append(torch.rand(k, dtype=torch.float64, device=cuda, generator=gen) - 0.5)
+    return ins, olds
+
+
+def _check_oracle(specs, ins, olds, outs):
+    for (dims, perm, f, g), u, y0, got in zip(specs, ins, olds, outs):
+        want = O.sort_generic(u.cpu().numpy(), dims, perm, f, g, out=y0.cpu().numpy().copy())
+        assert np.array_equal(got.cpu().numpy().view(np.uint64), want.view(np.uint64)), (dims, perm, f, g)
+
+
 def _run_both(cuda, seed, n):
     from spaghetty_gb300._lib import lib
     L = lib()
     specs = _specs(seed, n)
-    gen = torch.Generator(device=cuda)
-    gen.manual_seed(seed)
-    ins, out_ref, out_new = [], [], []
-    for dims, _, _, _ in specs:
-        k = int(np.prod(dims))
-        ins.append(torch.rand(k, dtype=torch.float64, device=cuda, generator=gen) - 0.5)
-        y = torch.rand(k, dtype=torch.float64, device=cuda, generator=gen) - 0.5
-        out_ref.append(y.clone())
-        out_new.append(y.clone())
+    ins, olds = _inputs(cuda, specs, seed)
+    out_ref = [y.clone() for y in olds]
+    out_new = [y.clone() for y in olds]
     stream = torch.cuda.current_stream().cuda_stream
-    # existing entry point (allocates its work list)
+    # the allocating entry point
     h = ctypes.c_void_p()
     ref = _entries(specs, ins, out_ref)
     assert L.spaghetty_batch_create(ctypes.cast(ref, ctypes.c_void_p), n, ctypes.byref(h)) == 0
@@ -77,6 +99,7 @@ def _run_both(cuda, seed, n):
     torch.cuda.synchronize()
     for a, b, sp in zip(out_ref, out_new, specs):
         assert torch.equal(a, b), sp
+    _check_oracle(specs, ins, olds, out_new)
 
 
 def test_noalloc_matches_allocating_entry_two_calls(cuda):
@@ -90,3 +113,34 @@ def test_noalloc_rejects_oversized_batch(cuda):
     arr = (BatchEntry * 1025)()
     rc = lib().spaghetty_sort_batch_noalloc(ctypes.cast(arr, ctypes.c_void_p), 1025, None)
     assert rc == 13
+
+
+_FIRST_CALL = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+sys.path.insert(0, sys.argv[2])
+import torch
+import test_zz_no_alloc as T
+from spaghetty_gb300._lib import lib
+cuda = torch.device("cuda", 0)
+for seed, n in ((303, 40), (404, 33)):
+    specs = T._specs(seed, n)
+    ins, olds = T._inputs(cuda, specs, seed)
+    outs = [y.clone() for y in olds]
+    arr = T._entries(specs, ins, outs)
+    rc = lib().spaghetty_sort_batch_noalloc(T.ctypes.cast(arr, T.ctypes.c_void_p), n,
+                                           T.ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == 0, rc
+    torch.cuda.synchronize()
+    T._check_oracle(specs, ins, olds, outs)
+print("first-call ok")
+"""
+
+
+def test_noalloc_first_call_in_fresh_process(cuda):
+    """The entry point as the first library call of a process (its per-device
+    set-up runs inside it), twice in a row, against the oracle."""
+    res = subprocess.run([sys.executable, "-c", _FIRST_CALL, ROOT, os.path.join(ROOT, "tests")],
+                         capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert "first-call ok" in res.stdout
