@@ -150,6 +150,19 @@ def np_sort(u: np.ndarray, dims: Sequence[int], perm: Sequence[int],
     return np.add(np.multiply(y, np.float64(acc_factor)), prod)
 
 
+def np_permuted(u: np.ndarray, dims: Sequence[int], perm: Sequence[int]) -> np.ndarray:
+    """The index map of old_sort_r alone (trunk/old_sort.f:54-58: element ia
+    of the input goes to position ib of the output): the input's elements in
+    output order, flat C order over (d_{p1}..d_{pr}), no arithmetic.  With
+    it, a sort is ``np.multiply(T, f)`` and a sortacc ``np.add(y,
+    np.multiply(T, f))`` -- np_sort's roundings -- so the full-size tests
+    permute once per permutation and reuse the result for every factor."""
+    dims = tuple(int(d) for d in dims)
+    axes = tuple(int(p) - 1 for p in perm)
+    x = np.asarray(u, dtype=np.float64).reshape(dims)
+    return np.ascontiguousarray(x.transpose(axes)).reshape(-1)
+
+
 def loop_dgemm(alpha: float, beta: float, a: np.ndarray, b: np.ndarray, c: np.ndarray,
                row_a: int, col_a: int, row_b: int, col_b: int, row_c: int, col_c: int,
                case: int) -> np.ndarray:

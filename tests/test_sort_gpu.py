@@ -3,7 +3,9 @@ reference (golden digests made by the reference's own nests) and the oracle,
 bit for bit.  Shapes are the sort4/sort6 configurations and the edge cases
 the reference's tester covers (trunk/generator2.py:446-629: every
 permutation, factors 1 and 37, the init_4d_array fixture), plus odd
-extents, unit dims, misaligned buffers and guard bands."""
+extents, unit dims, misaligned buffers and guard bands.  The full-size
+configurations (100^4, 16^6, 20^6, the non-cubic rank-6 shape, the batched
+mix) are checked in test_fullsize_gpu.py."""
 import ctypes
 import itertools
 import random
@@ -96,35 +98,6 @@ def test_sort4_sweep_sizes(cuda, dims):
                 check(got, want, (dims, perm, f, g))
 
 
-def test_sort4_100_full_size(cuda):
-    """100^4 (800 MB per tensor): oracle parity for three perms, and for every
-    perm the round trip sort(p) then sort(p^-1) restores the input exactly
-    (factor 0.5 then 2: exact power-of-two scalings)."""
-    dims = (100,) * 4
-    n = 100 ** 4
-    g = torch.Generator(device=cuda)
-    g.manual_seed(7)
-    u = torch.rand(n, dtype=torch.float64, device=cuda, generator=g) * 2 - 1
-    s = torch.empty_like(u)
-    r = torch.empty_like(u)
-    for perm in itertools.permutations((1, 2, 3, 4)):
-        inv = [0] * 4
-        for q, p in enumerate(perm):
-            inv[p - 1] = q + 1
-        sd = tuple(dims[p - 1] for p in perm)
-        sort_generic(u, s, dims, perm, 0.5, 0.0)
-        sort_generic(s, r, sd, inv, 2.0, 0.0)
-        torch.cuda.synchronize()
-        assert torch.equal(r, u), perm
-    uh = u.cpu().numpy()
-    yh = O.seeded_uniform(n, 9)
-    for perm in [(4, 3, 2, 1), (2, 4, 1, 3), (2, 3, 4, 1)]:
-        for gfac in (0.0, 1.0):
-            want = O.np_sort(uh, dims, perm, -0.5, gfac, out=yh)
-            got = gpu_sort(uh, dims, perm, -0.5, gfac, yh, cuda, via="generic")
-            check(got, want, ("100^4", perm, gfac))
-
-
 def test_sort6_all_perms_10(cuda):
     dims = (10,) * 6
     n = 10 ** 6
@@ -135,47 +108,6 @@ def test_sort6_all_perms_10(cuda):
         want = O.np_sort(u, dims, perm, -0.5, g, out=y)
         got = gpu_sort(u, dims, perm, -0.5, g, y, cuda)
         check(got, want, ("sort6 10^6", perm, g))
-
-
-def test_sort6_triples_16(cuda):
-    dims = (16,) * 6
-    n = 16 ** 6
-    u = O.seeded_uniform(n, 7)
-    y = O.seeded_uniform(n, 8)
-    for perm in TRIPLES_SORT6:
-        for g in (0.0, 1.0):
-            want = O.np_sort(u, dims, perm, 1.0 if g else -0.5, g, out=y)
-            got = gpu_sort(u, dims, perm, 1.0 if g else -0.5, g, y, cuda)
-            check(got, want, ("sort6 16^6", perm, g))
-
-
-def test_sort6_noncubic_and_20(cuda):
-    rnd = random.Random(11)
-    perms = rnd.sample(list(itertools.permutations(range(1, 7))), 24)
-    dims = (12, 20, 16, 20, 12, 16)
-    n = int(np.prod(dims))
-    u = O.seeded_uniform(n, 9)
-    y = O.seeded_uniform(n, 10)
-    for perm in perms:
-        for g in (0.0, 1.0):
-            want = O.np_sort(u, dims, perm, 0.5, g, out=y)
-            got = gpu_sort(u, dims, perm, 0.5, g, y, cuda)
-            check(got, want, ("sort6 noncubic", perm, g))
-    # 20^6 = 64M elements: round trip on the device for a few perms
-    dims = (20,) * 6
-    gen = torch.Generator(device=cuda)
-    gen.manual_seed(3)
-    du = torch.rand(20 ** 6, dtype=torch.float64, device=cuda, generator=gen) - 0.5
-    s = torch.empty_like(du)
-    r = torch.empty_like(du)
-    for perm in [(6, 5, 4, 3, 2, 1), (2, 6, 1, 5, 4, 3), (4, 5, 6, 1, 2, 3)]:
-        inv = [0] * 6
-        for q, p in enumerate(perm):
-            inv[p - 1] = q + 1
-        sort_generic(du, s, dims, perm, -1.0, 0.0)
-        sort_generic(s, r, dims, inv, -1.0, 0.0)
-        torch.cuda.synchronize()
-        assert torch.equal(r, du), perm
 
 
 def test_odd_extents_and_unit_dims(cuda):
