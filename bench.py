@@ -5,10 +5,11 @@ Workload (one "step"): the tce_sort_4 sweep -- all 24 permutations of a rank-4
 FP64 tensor at dims 20^4, 30^4, 50^4, 100^4 (800 MB per tensor) and
 (17,29,64,100), factors {1.0, -1.0, 0.5}, sort and sortacc: 720 launches.
 Inputs are seeded uniform(-1,1) FP64 resident in HBM.  Each launch is timed
-with CUDA events on its stream; before every launch whose tensors are smaller
-than 2x L2 (129 MB) the L2 is flushed by writing a 512 MB scratch buffer
-outside the timed events.  value = algorithmic bytes (16 B/element for sort,
-24 B/element for sortacc) / summed kernel time.
+with CUDA events on its stream; before every launch the L2 is flushed
+outside the timed events by a read-only pass over a 512 MB scratch buffer,
+which leaves the L2 holding clean lines (the previous kernel's dirty lines
+are written back during the flush, not during the timed kernel).  value = algorithmic bytes (16
+B/element for sort, 24 B/element for sortacc) / summed kernel time.
 
 e2e: the same sweep through the reference-facing C ABI (tce_sort_4 /
 tce_sortacc_4) with pinned HOST buffers, wall-clocked per call: each call
@@ -17,8 +18,9 @@ kernel, and copies the output back.
 
 --impl reference: the reference's own C loop nests (generated by
 trunk/generator2.py, built by oracle/make_ref.py with OpenMP over every host
-core), best of the 24 loop orders per permutation tuned at 30^4, timed over a
-bounded per-step sample of the same sweep.
+core), on the best of the 24 loop orders of each permutation and size (the
+table oracle/tune_ref_loops.py tunes on the host), timed over a bounded
+per-step sample of the same sweep.
 
 Multi-GPU: the sweep has no exchange step, so N ranks run N independent
 replicas ("replicas only"); value = all ranks' bytes / max rank time.
@@ -127,6 +129,21 @@ def sweep_cases():
     return cases
 
 
+def flush_l2(buf):
+    """Evict the L2 before a timed launch: a read-only reduction over `buf`
+    (4x the L2), so the L2 is left holding clean lines and the timed kernel
+    pays for no write-backs of earlier kernels' data."""
+    buf.sum()
+
+
+def needs_flush(n_elems):
+    """Every timed launch starts from a flushed L2: tensors near the L2's size
+    (16^6: 134 MB) would otherwise find part of their input there, or pay
+    for writing back the previous launch's dirty output lines, and even at
+    100^4 the previous launch's tail is in L2."""
+    return True
+
+
 def case_bytes(dims, acc):
     n = 1
     for d in dims:
@@ -184,8 +201,8 @@ def run_ours(args, ws, rank, local):
         evs = []
         for (dims, perm, f, acc) in cases:
             n = bufs[dims][2]
-            if n * 8 * 2 < 2 * L2_BYTES:
-                flush.fill_(1.0)
+            if needs_flush(n):
+                flush_l2(flush)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -298,6 +315,15 @@ def run_ours(args, ws, rank, local):
                 "launches": dom_n,
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, burst copy)"}
     breakdown = {k: round(v[1] / (v[0] / 1e3) / 1e9, 1) for k, v in per_size.items()}
+    # the identity permutation at each size is a plain streaming copy (the
+    # flat kernel): the floor that launch latency and the flush leave there
+    floor = {}
+    for (dims, perm, f, acc), (ms, b, kind) in detail.items():
+        if perm == (1, 2, 3, 4):
+            a = floor.setdefault("x".join(map(str, dims)), [0.0, 0])
+            a[0] += ms
+            a[1] += b
+    floor_gbs = {k: round(v[1] / (v[0] / 1e3) / 1e9, 1) for k, v in floor.items()}
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
@@ -305,10 +331,14 @@ def run_ours(args, ws, rank, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded uniform(-1,1) FP64 in HBM)",
         "config": {"workload": WORKLOAD, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "flushed (512 MB write) before every launch whose tensors are < 2x L2; "
-                         "100^4 tensors exceed L2"},
+                   "l2": "flushed before every timed launch (read-only pass over 512 MB, "
+                         "leaving clean lines)"},
         "gpu_launches": launches,
         "breakdown_gbs_by_size": breakdown,
+        "frac_of_peak_by_size": {k: round(v / peak, 4) for k, v in breakdown.items()},
+        "identity_copy_gbs_by_size": floor_gbs,
+        "frac_of_identity_copy_by_size": {k: round(breakdown[k] / floor_gbs[k], 4)
+                                          for k in breakdown if floor_gbs.get(k)},
         "frac_of_hbm_peak": round(value / ws / peak, 4),
         "roofline": roof,
         "e2e": e2e,
@@ -373,43 +403,56 @@ _CPU_STATE = {}
 
 
 def _cpu_setup():
-    """Build/load the reference nests, tune the loop order of every perm at
-    30^4 (all 24 orders, the reference's brute-force method,
-    trunk/generator2.py:581-598) once, and make the sweep's buffers."""
+    """Build/load the reference nests, pick the loop order of every
+    (perm, size) -- from oracle/ref_loop_orders.json when it was tuned on a
+    host like this one (all 24 orders timed per perm and size, the
+    reference's brute-force method, trunk/generator2.py:581-598), else by
+    timing the 24 orders once at 30^4 here -- and make the sweep's buffers."""
     import numpy as np
     from oracle import refnests as R
+    from oracle import tune_ref_loops as TR
     from spaghetty_gb300.workloads import PERMS4, SORT4_DIMS
     if _CPU_STATE:
         return _CPU_STATE
     if R.load() is None:
         return None
-    tdims = (30, 30, 30, 30)
-    n = 30 ** 4
     rng = np.random.default_rng(3)
-    u = rng.uniform(-1, 1, n)
-    s = np.zeros(n)
+    table = TR.load()
     best = {}
-    for perm in PERMS4:
-        bt, bl = 1e9, None
-        for lo in R.loops_for(4, perm):
-            R.call(perm, lo, u, s, tdims, 0.5, 0.0)
-            t0 = time.perf_counter()
-            R.call(perm, lo, u, s, tdims, 0.5, 0.0)
-            dt = time.perf_counter() - t0
-            if dt < bt:
-                bt, bl = dt, lo
-        best[perm] = bl
+    if table is not None:
+        for dims in SORT4_DIMS:
+            row = table["rank4"]["x".join(map(str, dims))]
+            for perm in PERMS4:
+                best[(dims, perm)] = row["".join(map(str, perm))]
+        how = "best of 24 loop orders per (perm, size), from the table tuned on this host type"
+    else:
+        tdims = (30, 30, 30, 30)
+        n = 30 ** 4
+        u = rng.uniform(-1, 1, n)
+        s = np.zeros(n)
+        for perm in PERMS4:
+            bt, bl = 1e9, None
+            for lo in R.loops_for(4, perm):
+                R.call(perm, lo, u, s, tdims, 0.5, 0.0)
+                t0 = time.perf_counter()
+                R.call(perm, lo, u, s, tdims, 0.5, 0.0)
+                dt = time.perf_counter() - t0
+                if dt < bt:
+                    bt, bl = dt, lo
+            for dims in SORT4_DIMS:
+                best[(dims, perm)] = bl
+        how = "best of 24 loop orders per perm, tuned here at 30^4"
     bufs = {}
     for dims in SORT4_DIMS:
         m = int(np.prod(dims))
         bufs[dims] = (rng.uniform(-1, 1, m), rng.uniform(-1, 1, m))
-    _CPU_STATE.update(best=best, bufs=bufs, R=R)
+    _CPU_STATE.update(best=best, bufs=bufs, R=R, how=how, table=table)
     return _CPU_STATE
 
 
 def cpu_sweep_sample(budget_s: float, threads: int | None = None, start: int = 0):
-    """The reference's C loop nests on the host cores (best loop order per
-    perm, tuned once at 30^4), timed over a bounded sample of the sweep
+    """The reference's C loop nests on the host cores (the tuned loop order
+    of each perm and size), timed over a bounded sample of the sweep
     starting at case `start`.  Returns (GB/s, cores, description, next)."""
     from spaghetty_gb300.workloads import PERMS4, SORT4_DIMS, SORT4_FACTORS
     if threads:
@@ -430,16 +473,69 @@ def cpu_sweep_sample(budget_s: float, threads: int | None = None, start: int = 0
         dims, perm, f, acc = order[i % len(order)]
         uu, ss = bufs[dims]
         t0 = time.perf_counter()
-        R.call(perm, best[perm], uu, ss, dims, f, 1.0 if acc else 0.0)
+        R.call(perm, best[(dims, perm)], uu, ss, dims, f, 1.0 if acc else 0.0)
         total_t += time.perf_counter() - t0
         total_b += case_bytes(dims, acc)
         calls += 1
         i += 1
     desc = ("reference generated C nests (trunk/generator2.py emitter, OpenMP over %d host "
-            "threads, gcc -O3 -ffp-contract=off), best of 24 loop orders per perm tuned at 30^4; "
+            "threads, gcc -O3 -ffp-contract=off), %s; "
             "%d calls of the sweep (24 perms x 5 sizes x f{1,-1,0.5} x sort/sortacc, the five "
-            "sizes interleaved, from case %d) within a %.0f s budget" % (cores, calls, start % len(order), budget_s))
+            "sizes interleaved, from case %d) within a %.0f s budget"
+            % (cores, st["how"], calls, start % len(order), budget_s))
     return total_b / total_t / 1e9, cores, desc, i
+
+
+def cpu_sort6_baseline(budget_s):
+    """The reference's rank-6 C nests (trunk/generator6.py emitter) on the
+    host cores at 16^6 for the 54 CCSD(T) perms, sort (f = -0.5) and sortacc
+    (f = 1), each perm on its best emitted loop order (the committed table,
+    else timed here), over a bounded sample."""
+    try:
+        import numpy as np
+        from oracle import refnests as R
+        from oracle import tune_ref_loops as TR
+        from spaghetty_gb300.workloads import TRIPLES_SORT6
+        if R.load() is None:
+            return {"value": None, "unit": UNIT, "error": "reference nests unavailable"}
+        dims = (16,) * 6
+        n = 16 ** 6
+        rng = np.random.default_rng(6)
+        u, s = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+        table = TR.load()
+        best = {}
+        for perm in TRIPLES_SORT6:
+            key = "".join(map(str, perm))
+            if table is not None and key in table["rank6"]["16x16x16x16x16x16"]:
+                best[perm] = table["rank6"]["16x16x16x16x16x16"][key]
+                continue
+            bt = None
+            for lo in R.loops_for(6, perm):
+                t0 = time.perf_counter()
+                R.call(perm, lo, u, s, dims, 0.5, 0.0)
+                dt = time.perf_counter() - t0
+                if bt is None or dt < bt:
+                    bt, best[perm] = dt, lo
+        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        total_b, total_t, calls = 0, 0.0, 0
+        t_start = time.perf_counter()
+        order = [(p, acc) for p in TRIPLES_SORT6 for acc in (False, True)]
+        while calls < len(order) and time.perf_counter() - t_start <= budget_s:
+            perm, acc = order[calls]
+            t0 = time.perf_counter()
+            R.call(perm, best[perm], u, s, dims, 1.0 if acc else -0.5, 1.0 if acc else 0.0)
+            total_t += time.perf_counter() - t0
+            total_b += n * (24 if acc else 16)
+            calls += 1
+        return {"value": round(total_b / total_t / 1e9, 2), "unit": UNIT, "cores": cores,
+                "kind": "reference",
+                "sample": "reference generated C nests (trunk/generator6.py emitter, OpenMP over %d "
+                          "host threads, gcc -O3 -ffp-contract=off), best of the emitted loop orders "
+                          "per perm (%s); %d calls: the 54 CCSD(T) perms at 16^6, sort and sortacc, "
+                          "within a %.0f s budget"
+                          % (cores, "committed table" if table else "timed here", calls, budget_s)}
+    except Exception as e:  # noqa: BLE001
+        return {"value": None, "unit": UNIT, "error": str(e)[:200]}
 
 
 def cpu_baseline(budget_s):
@@ -559,47 +655,62 @@ def _timed_events(fn, reps, stream):
 
 
 def run_sort6(args, dev):
-    """tce_sort_6 sweep sample: all 720 perms at 10^6, the 54 CCSD(T) perms at
-    16^6 and 20^6, and 48 seeded perms at (12,20,16,20,12,16); sort and
-    sortacc (f = -0.5 / 1.0).  Per-size effective GB/s (L2 flushed before
-    every launch of tensors under 2x L2)."""
-    import random
+    """The tce_sort_6 configuration: all 720 perms at 10^6, 16^6, 20^6 and
+    (12,20,16,20,12,16), sort (f = -0.5) and sortacc (f = 1.0), one timed
+    launch each after an untimed pass that builds the plans.  Per shape:
+    effective GB/s over all perms, its fraction of the HBM peak, the identity
+    perm's GB/s (a plain streaming copy: the floor that launch latency leaves
+    at that size) and the 54 CCSD(T) perms' GB/s.  L2 flushed (read-only)
+    before every timed launch."""
     import torch
     import spaghetty_gb300 as S
-    from spaghetty_gb300.workloads import PERMS6, TRIPLES_SORT6
-    rnd = random.Random(6)
-    groups = [((10,) * 6, PERMS6), ((16,) * 6, TRIPLES_SORT6), ((20,) * 6, TRIPLES_SORT6),
-              ((12, 20, 16, 20, 12, 16), rnd.sample(PERMS6, 48))]
+    from spaghetty_gb300.workloads import PERMS6, SORT6_DIMS, TRIPLES_SORT6
+    triples = set(TRIPLES_SORT6)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     stream = torch.cuda.current_stream(dev)
+    peak, _ = peaks()
     out = {}
-    for dims, perms in groups:
+    for dims in SORT6_DIMS:
         n = 1
         for d in dims:
             n *= d
         u = torch.rand(n, dtype=torch.float64, device=dev) - 0.5
         y = torch.rand(n, dtype=torch.float64, device=dev) - 0.5
-        tot_b = 0
         evs = []
         # events collected and read at the end: the host runs ahead of the
-        # GPU, so each pair brackets only its kernel
+        # GPU (each launch follows a flush), so each pair brackets only its
+        # kernel
         for rep in range(2):
-            for perm in perms:
+            for perm in PERMS6:
                 for acc in (False, True):
-                    if n * 16 < 2 * L2_BYTES:
-                        flush.fill_(1.0)
+                    if needs_flush(n):
+                        flush_l2(flush)
                     e0 = torch.cuda.Event(enable_timing=True)
                     e1 = torch.cuda.Event(enable_timing=True)
                     e0.record(stream)
                     S.sort_generic(u, y, dims, perm, 1.0 if acc else -0.5, 1.0 if acc else 0.0)
                     e1.record(stream)
                     if rep:
-                        evs.append((e0, e1))
-                        tot_b += n * (24 if acc else 16)
+                        evs.append((perm, acc, e0, e1))
         torch.cuda.synchronize()
-        tot_t = sum(a.elapsed_time(b) for a, b in evs) / 1e3
-        out["x".join(map(str, dims))] = {"gbs": round(tot_b / tot_t / 1e9, 1), "launches": 2 * len(perms)}
+        acc_b = {"all": [0, 0.0], "triples": [0, 0.0], "identity": [0, 0.0]}
+        for perm, acc, e0, e1 in evs:
+            t = e0.elapsed_time(e1) / 1e3
+            b = n * (24 if acc else 16)
+            for k, on in (("all", True), ("triples", perm in triples), ("identity", perm == PERMS6[0])):
+                if on:
+                    acc_b[k][0] += b
+                    acc_b[k][1] += t
+        g = {k: v[0] / v[1] / 1e9 for k, v in acc_b.items()}
+        out["x".join(map(str, dims))] = {
+            "gbs": round(g["all"], 1), "frac_of_peak": round(g["all"] / peak, 4),
+            "identity_copy_gbs": round(g["identity"], 1),
+            "frac_of_identity_copy": round(g["all"] / g["identity"], 4),
+            "triples_gbs": round(g["triples"], 1), "launches": len(evs),
+            "l2": "flushed before every launch"}
         del u, y
+    if not args.no_cpu:
+        out["cpu_baseline_16^6_triples"] = cpu_sort6_baseline(min(20.0, args.cpu_seconds))
     return out
 
 
@@ -644,7 +755,11 @@ def run_fused(args, dev):
 
 def run_autograd(args, dev):
     """y = sum_k f_k * permute_k(x) over 3 seeded perms and its hand-written
-    backward, forward+backward GB/s (each pass: one sort + two sortaccs)."""
+    backward, one fused launch per direction (spaghetty_sort_fused).
+    fwd_bwd_gbs counts the algorithmic bytes of the operation as a sort plus
+    two sortaccs per direction (2 x 64 B/element); fused_traffic_gbs the
+    fused kernels' own (3 reads of the source and one write per direction,
+    2 x 32 B/element)."""
     import torch
     from spaghetty_gb300.autograd import permute_sum
     stream = torch.cuda.current_stream(dev)
@@ -666,6 +781,7 @@ def run_autograd(args, dev):
             step()
         t = _timed_events(step, 10, stream)
         res["x".join(map(str, dims))] = {"fwd_bwd_gbs": round(2 * (16 + 2 * 24) * n / t / 1e9, 1),
+                                          "fused_traffic_gbs": round(2 * (3 * 8 + 8) * n / t / 1e9, 1),
                                           "ms": round(t * 1e3, 4)}
     return res
 
@@ -682,7 +798,7 @@ def run_contract(args, dev):
     from spaghetty_gb300.contract import contract_4x4
     stream = torch.cuda.current_stream(dev)
     res = {}
-    for d in (16, 24):
+    for d in (16, 24, 32):
         d1 = d2 = d3 = d4 = d5 = d6 = d
         M, N, K = d1 * d2, d3 * d4, d5 * d6
         t = torch.rand(d5 * d6 * d1 * d2, dtype=torch.float64, device=dev) - 0.5
@@ -705,13 +821,14 @@ def run_contract(args, dev):
 
         row = {}
         for name, fn in (("fused_exact", lambda: fused("exact")), ("fused_fma", lambda: fused("fma")),
-                         ("unfused_cublas", unfused)):
+                         ("fused_mma", lambda: fused("mma")), ("unfused_cublas", unfused)):
             for _ in range(3):
                 fn()
             tm = _timed_events(fn, 10, stream)
             row[name] = {"ms": round(tm * 1e3, 4), "gflops": round(2.0 * M * N * K / tm / 1e9, 1)}
         row["fma_vs_unfused"] = round(row["unfused_cublas"]["ms"] / row["fused_fma"]["ms"], 2)
         row["exact_vs_unfused"] = round(row["unfused_cublas"]["ms"] / row["fused_exact"]["ms"], 2)
+        row["mma_vs_fma"] = round(row["fused_fma"]["ms"] / row["fused_mma"]["ms"], 2)
         res["%d^6" % d] = row
         del t, v, c, a_s, b_s, c_s
     return res
@@ -761,8 +878,8 @@ def run_case(args):
     g = 0.0 if op == 0 else 1.0
     times = []
     for r in range(args.warmup + args.steps):
-        if n * 16 < 2 * L2_BYTES:
-            flush.fill_(1.0)
+        if needs_flush(n):
+            flush_l2(flush)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()

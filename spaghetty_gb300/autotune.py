@@ -179,7 +179,8 @@ def clear():
 def time_case(dims, perm, op, reps=5, device=None, flush_bytes=512 << 20, bufs=None):
     """Median kernel time (s) of one sort on device buffers, L2 flushed
     before every launch (so that no launch finds the previous one's tail in
-    L2, which would favour some box orders over others)."""
+    L2, which would favour some box orders over others) by a read-only pass
+    over a scratch buffer, which leaves clean lines behind."""
     import torch
     from .sort import sort_generic
     dev = device or torch.device("cuda", torch.cuda.current_device())
@@ -195,7 +196,7 @@ def time_case(dims, perm, op, reps=5, device=None, flush_bytes=512 << 20, bufs=N
     g = 0.0 if op == 0 else (1.0 if op == 1 else 2.0)
     times = []
     for r in range(reps + 1):
-        flush.fill_(1.0)
+        flush.sum()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
@@ -390,7 +391,7 @@ def tune_batched(cache, n=4096, seed=2024, budget_bytes=6 << 30, reps=3, verbose
         try:
             ts = []
             for r in range(reps + 1):
-                flush.fill_(1.0)
+                flush.sum()
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record()
@@ -453,7 +454,7 @@ def tune_batched(cache, n=4096, seed=2024, budget_bytes=6 << 30, reps=3, verbose
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--sweep", default="sort4",
-                    choices=["sort4", "sort6-triples", "sort6-sample", "batched", "case"])
+                    choices=["sort4", "sort6-triples", "sort6-sample", "random", "batched", "case"])
     ap.add_argument("--dims", default="100,100,100,100")
     ap.add_argument("--perm", default="4,3,2,1")
     ap.add_argument("--ops", default="0,1")
@@ -468,6 +469,20 @@ def main():
         probs = [(d, p) for d in SORT4_DIMS for p in PERMS4]
     elif args.sweep == "sort6-triples":
         probs = [((16,) * 6, p) for p in TRIPLES_SORT6]
+    elif args.sweep == "random":
+        # seeded shapes outside the configurations (the data the planner's
+        # default rules are fitted on): rank 4 with extents in [8, 64],
+        # rank 6 with extents in [6, 20], random permutations
+        import random
+        rnd = random.Random(4646)
+        probs = []
+        for i in range(48):
+            r = 4 if i % 2 == 0 else 6
+            dims = tuple(rnd.randint(8, 64) if r == 4 else rnd.randint(6, 20) for _ in range(r))
+            perm = list(range(1, r + 1))
+            while perm == sorted(perm):
+                rnd.shuffle(perm)
+            probs.append((dims, tuple(perm)))
     elif args.sweep == "sort6-sample":
         # the sort6 configuration's bench sample: triples perms at 16^6 and
         # 20^6, 48 seeded perms at the non-cubic shape
