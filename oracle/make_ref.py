@@ -37,7 +37,8 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_TRUNK = "/root/reference/trunk"
+# the reference checkout's trunk/ (SPAGHETTY_REFERENCE_DIR names the checkout)
+REF_TRUNK = os.path.join(os.environ.get("SPAGHETTY_REFERENCE_DIR", "/root/reference"), "trunk")
 LIB = os.path.join(OUT, "libref_nests.so")
 
 TRIPLES = None  # filled from the reference's nwchem_triples_usage()

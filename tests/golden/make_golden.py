@@ -4,7 +4,8 @@ Runs the C code that the reference's emitters write (generate_cfunction in
 trunk/generator2.py:48-130 and trunk/generator6.py:61-134, built by
 oracle/make_ref.py from the reference checkout) on deterministic inputs and
 records the SHA-256 of every output.  The committed JSON is what pins the
-oracle (tests/test_oracle.py) and the GPU kernels (tests/test_golden_gpu.py)
+oracle (tests/test_oracle.py) and the GPU kernels
+(tests/test_sort_gpu.py::test_golden_digests_all_perms)
 to the reference without needing the reference checkout at test time.
 
 Cases (every permutation; small shapes that hit odd extents and unit dims):
