@@ -229,6 +229,11 @@ const char *spaghetty_error_string(int code);
  * host memory, move them in slabs along the output's slowest index through
  * a two-stream upload / sort / download pipeline instead. */
 #define SPAGHETTY_OPT_HOST_PIPELINE 2
+/* SPAGHETTY_OPT_TMA_SKEW (default 1): TMA-staged plans may rotate the
+ * permute step's slot map to spread its shared-memory accesses over the
+ * banks (chosen per plan by simulating them); 0 plans without the rotation.
+ * Changing it drops the cached plans. */
+#define SPAGHETTY_OPT_TMA_SKEW 3
 int spaghetty_set_option(int option, int value);
 
 /* Synchronise the current device and report (then clear) the kernels'

@@ -188,6 +188,10 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
 }
 
 int choose_skew(Plan *pl);
+// SPAGHETTY_OPT_TMA_SKEW: 1 (default) lets choose_skew rotate the permute
+// step's slot map where the bank simulation favours it, 0 plans every TMA
+// kernel without skew.
+int g_tma_skew = 1;
 
 // Switch a built tiled plan to the TMA-staged kernel with the given shape.
 int to_tma(Plan *pl, int threads, int ept, int stages, bool strict) {
@@ -247,7 +251,7 @@ static int64_t tma_permute_wavefronts(const Plan &pl, const TmaParams &tp) {
 // takes the fewest simulated wavefronts (ties keep the simpler mapping).
 int choose_skew(Plan *pl) {
     pl->sk_stride = pl->sk_len = pl->sk_mul = 0;
-    if (pl->kind != KIND_TMA || pl->kp.vol >= 65535 || pl->fo.P[pl->fo.rank - 1] == pl->fo.rank - 1)
+    if (!g_tma_skew || pl->kind != KIND_TMA || pl->kp.vol >= 65535 || pl->fo.P[pl->fo.rank - 1] == pl->fo.rank - 1)
         return SPAGHETTY_OK;   // same-order tiles: the permute step is the identity
     TmaParams tp;
     std::memset(&tp, 0, sizeof(tp));
@@ -949,6 +953,12 @@ int spaghetty_set_option(int option, int value) {
     }
     if (option == SPAGHETTY_OPT_HOST_PIPELINE) {
         g_pipeline = value ? 1 : 0;
+        return SPAGHETTY_OK;
+    }
+    if (option == SPAGHETTY_OPT_TMA_SKEW) {
+        std::lock_guard<std::mutex> lk(g_plans_mu);
+        g_tma_skew = value ? 1 : 0;
+        g_plans.clear();
         return SPAGHETTY_OK;
     }
     return SPAGHETTY_ERR_CONFIG;

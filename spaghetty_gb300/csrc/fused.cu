@@ -82,7 +82,7 @@ __device__ __forceinline__ double spg_fused_apply(int op, double acc, double x, 
     }
 }
 
-__global__ void __launch_bounds__(SPG_FUSED_NT)
+__global__ void __launch_bounds__(SPG_FUSED_NT, 1)
 spg_fused_sortacc(double *__restrict__ out, const __grid_constant__ FusedParams p) {
     extern __shared__ __align__(16) unsigned char smem[];
     // layout: int32 off[nsrc][vol] | uint16 slot[nsrc][vol] | double buf[2][tile]
@@ -247,7 +247,7 @@ __device__ __forceinline__ void spg_ft_coords(const FusedTmaParams &p, int map, 
 }
 
 template <int NT, int EPT, int S>
-__global__ void __launch_bounds__(SPG_FT_BLOCK(NT))
+__global__ void __launch_bounds__(SPG_FT_BLOCK(NT), 1)
 spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__ FusedTmaParams p) {
     extern __shared__ __align__(1024) unsigned char smem_raw0[];
     const uint32_t raw = (uint32_t)__cvta_generic_to_shared(smem_raw0);

@@ -154,7 +154,7 @@ __device__ __forceinline__ void spg_mbar_arrive(uint32_t addr) {
 #define SPG_TMA_BLOCK(NT) ((NT) + 64)
 
 template <int NT, int EPT, int OP, int S>
-__global__ void __launch_bounds__(SPG_TMA_BLOCK(NT))
+__global__ void __launch_bounds__(SPG_TMA_BLOCK(NT), 1)
 spg_tiled_tma(const __grid_constant__ CUtensorMap tmap_in,
               const __grid_constant__ CUtensorMap tmap_out,
               const __grid_constant__ KParams p, const __grid_constant__ TmaParams tp) {
