@@ -349,10 +349,14 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
     // Default plans, chosen from the GB300 autotuner's timings of every
     // candidate over the sort4 sweep, the sort6 sample and random shapes:
     //  - transposes: the TMA-staged kernel on the greedy box with 32-double
-    //    rows on both sides grown towards 4096 elements, the smallest CTA
+    //    rows on both sides grown towards 1024 elements, the smallest CTA
     //    (128x8, 256x8, 256x16) that holds it, 3 load stages (2 when 3 do
     //    not fit); otherwise the register-staged tiled kernel on the greedy
-    //    box with 16/32-double rows towards 512 elements;
+    //    box with 16/32-double rows towards 512 elements.  (Of the rules
+    //    (input rows, output rows, volume, stages) timed on 184 problems,
+    //    ranks 4 and 6, this one came within 6% of each problem's best
+    //    candidate on average; towards 4096 elements, one CTA per SM, was
+    //    15% off: 4.7 against 5.6 TB/s at 16^6.)
     //  - the stride-1 index unchanged: the same-order TMA plan on a box of
     //    at most 1K elements, 128 threads x 8, 3 load stages (else 2).
     // Host-mapped (zero-copy) and misaligned buffers cannot use the bulk
@@ -362,7 +366,7 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
         int box[SPG_MAXR];
         Plan tp;
         bool done = false;
-        if (spg_box_greedy(fo, 32, 32, 4096, 4096, box) == SPAGHETTY_OK) {
+        if (spg_box_greedy(fo, 32, 32, 1024, 4096, box) == SPAGHETTY_OK) {
             // the bulk copies move whole 16-byte units along both stride-1
             // dims: round an odd partial box length there up to even
             for (const int d : {fo.rank - 1, fo.P[fo.rank - 1]})
