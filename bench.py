@@ -702,6 +702,13 @@ def run_sort6(args, dev):
                     acc_b[k][0] += b
                     acc_b[k][1] += t
         g = {k: v[0] / v[1] / 1e9 for k, v in acc_b.items()}
+        if args.detail:
+            with open(args.detail, "a") as fh:
+                for perm, acc, e0, e1 in evs:
+                    t = e0.elapsed_time(e1) / 1e3
+                    fh.write(json.dumps({"dims": list(dims), "perm": list(perm), "acc": acc,
+                                         "kind": S.plan(dims, perm, int(acc))["kind"],
+                                         "gbs": round(n * (24 if acc else 16) / t / 1e9, 1)}) + "\n")
         out["x".join(map(str, dims))] = {
             "gbs": round(g["all"], 1), "frac_of_peak": round(g["all"] / peak, 4),
             "identity_copy_gbs": round(g["identity"], 1),

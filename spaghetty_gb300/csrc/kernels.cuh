@@ -70,6 +70,75 @@ __device__ __forceinline__ double spg_neg_voted(double x, const SpgFactor &F) {
     return r;
 }
 
+// x * f, rounded to nearest even, for any normal f, in 32-bit integer
+// operations: the IEEE 754 binary64 product by the schoolbook method for
+// software floating point (exact product of the two 53-bit significands,
+// normalisation by one bit, round to nearest with ties to even from the round
+// bit and the sticky bits, exponents added; IEEE 754-2008 sec. 4.3.1 and 5.4.1).
+// The 106-bit significand product is built from four 32 x 32-bit products
+// (x's significand as 21 + 32 bits, f's precomputed on the host the same way)
+// with carry-chained 32-bit adds.  The packed result's rounding increment
+// carries into the exponent field, which also gives the right infinity when
+// rounding overflows.  `exact` is cleared where this path does not apply:
+// x subnormal, inf or NaN, a product outside the normal range before
+// rounding, or f itself not normal (F.mul_ok = 0); x = +-0 gives a signed
+// zero.  GB300 issues FP64 multiplies at a small fraction of its 32-bit
+// integer rate, but this costs about 40 integer instructions per element:
+// measured on GB300 with f = 0.3, it is faster only in the flat streaming
+// kernel (100^4 identity: sortacc 6683 against 5969 GB/s, sort 6283 against
+// 6200), and slower in the staged kernels, whose permute threads are issue
+// bound (100^4 perm 4321 on the TMA kernel: sort 4872 against 5730; the
+// batched mix 2958 against 3470), which keep the rounded multiply.
+__device__ __forceinline__ double spg_mul_int(double x, const SpgFactor &F, bool &exact) {
+    const uint32_t hi = (uint32_t)__double2hiint(x);
+    const uint32_t lo = (uint32_t)__double2loint(x);
+    const uint32_t ex = (hi >> 20) & 0x7FFu;
+    const uint32_t xh = (hi & 0xFFFFFu) | 0x100000u;
+    // P = (xh 2^32 + lo)(mhi 2^32 + mlo) as the words w3:w2:w1:w0, P < 2^106
+    const uint32_t a0 = lo * F.mlo, a1 = __umulhi(lo, F.mlo);
+    const uint32_t b0 = xh * F.mlo, b1 = __umulhi(xh, F.mlo);
+    const uint32_t c0 = lo * F.mhi, c1 = __umulhi(lo, F.mhi);
+    const uint32_t d0 = xh * F.mhi, d1 = __umulhi(xh, F.mhi);
+    uint32_t w1, w2, w3;
+    asm("add.cc.u32 %0, %3, %4;\n\t"
+        "addc.cc.u32 %1, %5, %6;\n\t"
+        "addc.u32 %2, %7, 0;\n\t"
+        "add.cc.u32 %0, %0, %8;\n\t"
+        "addc.cc.u32 %1, %1, %9;\n\t"
+        "addc.u32 %2, %2, 0;"
+        : "=&r"(w1), "=&r"(w2), "=&r"(w3)
+        : "r"(a1), "r"(b0), "r"(b1), "r"(d0), "r"(d1), "r"(c0), "r"(c1));
+    // P in [2^104, 2^106): s = 1 when bit 105 (bit 9 of w3) is set; the
+    // significand is P >> (52 + s), the round bit the one below it
+    const uint32_t s = (w3 >> 9) & 1u;
+    const uint32_t sh = 20u + s;
+    const uint32_t sig_lo = __funnelshift_r(w1, w2, sh);
+    const uint32_t sig_hi = __funnelshift_r(w2, w3, sh);      // 21 bits, leading one at bit 20
+    const uint32_t rnd = (w1 >> (sh - 1u)) & 1u;
+    const uint32_t sticky = (w1 & ((1u << (sh - 1u)) - 1u)) | a0;
+    const uint32_t inc = rnd & ((sticky != 0u ? 1u : 0u) | (sig_lo & 1u));
+    const uint32_t e = ex + (uint32_t)F.ebias + s;             // biased exponent of the result
+    uint32_t rlo, rhi;
+    asm("add.cc.u32 %0, %2, %3;\n\t"
+        "addc.u32 %1, %4, 0;"
+        : "=r"(rlo), "=r"(rhi)
+        : "r"(sig_lo), "r"(inc), "r"((e << 20) + sig_hi - 0x100000u));
+    const uint32_t sign = (hi ^ F.sgn_hi) & 0x80000000u;
+    const bool zero = ((hi & 0x7FFFFFFFu) | lo) == 0u;
+    const bool normal = ex - 1u < 2046u && e - 1u < 2046u;
+    exact = exact && F.mul_ok != 0u && (normal || zero);
+    return zero ? __hiloint2double((int)sign, 0) : __hiloint2double((int)(rhi | sign), (int)rlo);
+}
+
+__device__ __forceinline__ double spg_mul(double x, const SpgFactor &F) {
+    bool exact = true;
+    double r = spg_mul_int(x, F, exact);
+    if (__any_sync(__activemask(), !exact)) {
+        if (!exact) r = spg_dmul_branch(x, F.f);
+    }
+    return r;
+}
+
 // Per-element forms: the rare inexact cases take the rounded multiply behind
 // a warp vote, so that it is a real branch and the bits always equal
 // __dmul_rn(x, f).
@@ -432,6 +501,14 @@ spg_direct(const double *__restrict__ in, double *__restrict__ out,
         spg_direct_box<NT, EPT, OP>(p, tb, in, out, t);
 }
 
+// The flat kernel's arithmetic: arbitrary factors on the integer multiply.
+template <int OP>
+__device__ __forceinline__ double spg_apply_flat(double x, double y, const SpgFactor &F) {
+    if (OP == OP_SORT_ANY) return spg_mul(x, F);
+    if (OP == OP_ACC_ANY) return __dadd_rn(y, spg_mul(x, F));
+    return spg_apply<OP>(x, y, F);
+}
+
 // ---------------------------------------------------------------------------
 // Flat: n contiguous elements, identity order.  VEC = 2 uses 16-byte
 // accesses (both pointers 16-byte aligned); the odd tail element is handled
@@ -458,8 +535,8 @@ spg_flat(const double *__restrict__ in, double *__restrict__ out, int64_t n,
 #pragma unroll
             for (int u = 0; u < 4; ++u) {
                 double2 r;
-                r.x = spg_apply<OP>(x[u].x, y[u].x, fac);
-                r.y = spg_apply<OP>(x[u].y, y[u].y, fac);
+                r.x = spg_apply_flat<OP>(x[u].x, y[u].x, fac);
+                r.y = spg_apply_flat<OP>(x[u].y, y[u].y, fac);
                 __stcs(out2 + j + u * stride, r);
             }
         }
@@ -468,20 +545,20 @@ spg_flat(const double *__restrict__ in, double *__restrict__ out, int64_t n,
             double2 y = make_double2(0.0, 0.0);
             if (spg_reads_out<OP>::value) y = __ldcs(out2 + j);
             double2 r;
-            r.x = spg_apply<OP>(x.x, y.x, fac);
-            r.y = spg_apply<OP>(x.y, y.y, fac);
+            r.x = spg_apply_flat<OP>(x.x, y.x, fac);
+            r.y = spg_apply_flat<OP>(x.y, y.y, fac);
             __stcs(out2 + j, r);
         }
         if ((n & 1) && i0 == 0) {
             const double x = in[n - 1];
             const double y = spg_reads_out<OP>::value ? out[n - 1] : 0.0;
-            out[n - 1] = spg_apply<OP>(x, y, fac);
+            out[n - 1] = spg_apply_flat<OP>(x, y, fac);
         }
     } else {
         for (int64_t j = i0; j < n; j += stride) {
             const double x = __ldcs(in + j);
             const double y = spg_reads_out<OP>::value ? __ldcs(out + j) : 0.0;
-            __stcs(out + j, spg_apply<OP>(x, y, fac));
+            __stcs(out + j, spg_apply_flat<OP>(x, y, fac));
         }
     }
 }

@@ -130,6 +130,18 @@ SpgFactor spg_make_factor(double f, double g) {
             F.erange = (uint32_t)(ehi - elo + 1) << 20;
         }
     }
+    // the integer multiply's operand: f normal (biased exponent 1..2046)
+    uint64_t bits;
+    std::memcpy(&bits, &f, sizeof(bits));
+    const int ef = (int)((bits >> 52) & 0x7FF);
+    if (ef >= 1 && ef <= 2046) {
+        const uint64_t m = (bits & ((1ull << 52) - 1)) | (1ull << 52);
+        F.mhi = (uint32_t)(m >> 32);
+        F.mlo = (uint32_t)m;
+        F.ebias = ef - 1023;
+        F.mul_ok = 1;
+        if (fc > 2) F.sgn_hi = std::signbit(f) ? 0x80000000u : 0u;
+    }
     return F;
 }
 

@@ -67,6 +67,14 @@ struct SpgFactor {
     // high words (sign bit cleared) of the x for which x and x*2^k are both
     // normal: elo <= hi(x) & 0x7FFFFFFF < elo + erange (erange 0: none)
     uint32_t elo, erange;
+    // any other normal f, for the integer multiply (spg_mul_int): f's 53-bit
+    // significand with its leading one as two 32-bit words (mhi holds the top
+    // 21 bits), its biased exponent minus 1023, and its sign in the high
+    // word; mul_ok = 0 (f zero, subnormal, inf or NaN) sends every element
+    // to the rounded multiply
+    uint32_t mhi, mlo;
+    int32_t ebias;
+    uint32_t mul_ok;
 };
 
 struct KParams {

@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
+from spaghetty_gb300 import plan
 from spaghetty_gb300.workloads import batched_mix
 from tests._util import bits_equal, first_mismatch
 
@@ -195,12 +196,18 @@ def test_large_sorts_run_as_their_own_launches(cuda):
     big = [{"dims": (64, 40, 40, 48), "perm": (2, 4, 3, 1), "factor": -0.5, "g": 0.0},
            {"dims": (16, 12, 12, 16, 8, 16), "perm": (6, 5, 4, 3, 2, 1), "factor": 1.0, "g": 1.0},
            {"dims": (40, 64, 48, 40), "perm": (1, 3, 2, 4), "factor": 0.75, "g": -0.25},
-           {"dims": (16, 10, 12, 16, 8, 18), "perm": (3, 2, 6, 1, 5, 4), "factor": 1.0, "g": 1.0}]
+           # odd extents only: no bulk tensor copy can describe its rows,
+           # so it is planned on another kernel and stays on the work list
+           {"dims": (15, 17, 13, 11, 9, 13), "perm": (3, 2, 6, 1, 5, 4), "factor": 1.0, "g": 1.0}]
     specs = specs[:20] + big + specs[20:]
     jobs, host = make_jobs(specs, cuda, 400)
     b = Batch(jobs)
     info = b.info()
-    assert info["jobs"] == 41 and info["launches"] == 4   # the last large one stays on the work list
+    opclass = {0.0: 0, 1.0: 1}
+    direct = [sp for sp in big if int(np.prod(sp["dims"])) >= 1 << 22 and
+              plan(sp["dims"], sp["perm"], opclass.get(sp["g"], 2))["kind"] == "tma"]
+    assert len(direct) == 3 and big[3] not in direct
+    assert info["jobs"] == 44 - len(direct) and info["launches"] == len(direct) + 1
     b.capture()          # warm-up launch, then capture
     b.replay()           # the sorts ran twice: sortaccs accumulate twice
     assert b.status() == 0
