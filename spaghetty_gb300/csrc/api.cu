@@ -18,6 +18,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <iterator>
 #include <map>
 #include <mutex>
 #include <string>
@@ -140,10 +141,12 @@ std::string tune_key(const Folded &fo, int op) {
 void autoload_tune_file();
 
 // Plans are cached by (rank, dims, perm, op, SM count): NWChem repeats the
-// same few shapes thousands of times, and planning (box search, pad
-// simulation) costs microseconds.  Cleared whenever an override changes.
+// same few shapes thousands of times, and planning (box search, bank
+// simulations) costs up to a few hundred microseconds.  Cleared whenever an
+// override changes; past kPlanCacheMax entries half of them are dropped.
 std::unordered_map<std::string, Plan> g_plans;
 std::mutex g_plans_mu;
+const size_t kPlanCacheMax = 16384;   // about 1.3 KB per entry
 
 std::string plan_key(int rank, const int *dims, const int *perm, int op, int sms) {
     std::string k;
@@ -181,7 +184,13 @@ int make_plan(int rank, const int *dims, const int *perm, double f, double g, in
     int rc = make_plan_uncached(rank, dims, perm, f, g, sms, allow_tma, host_link, pl);
     if (rc == SPAGHETTY_OK) {
         std::lock_guard<std::mutex> lk(g_plans_mu);
-        if (g_plans.size() > 8192) g_plans.clear();
+        if (g_plans.size() >= kPlanCacheMax) {
+            // drop every other entry rather than all: a working set just
+            // above the limit then re-plans a part of its shapes, not all
+            bool drop = true;
+            for (auto it = g_plans.begin(); it != g_plans.end(); drop = !drop)
+                it = drop ? g_plans.erase(it) : std::next(it);
+        }
         g_plans[key] = *pl;
     }
     return rc;
@@ -215,33 +224,30 @@ int to_tma(Plan *pl, int threads, int ept, int stages, bool strict) {
 // 8-byte reads of the input tile at lin and the writes of the output tile at
 // e (a sortacc's reads of the old output use the same words as the writes).
 // A half warp's accesses take one wavefront per access of the busiest bank
-// pair (distinct words; equal words are one access).
-static int64_t tma_permute_wavefronts(const Plan &pl, const TmaParams &tp) {
+// pair.  Slot -> e and e -> lin are bijections, so a half warp's 16 words
+// are distinct and the count needs no de-duplication.  lin0[e]: the
+// input-tile element of output-tile element e (spg_walk, computed once).
+static int64_t tma_permute_wavefronts(const Plan &pl, const TmaParams &tp, const std::vector<int32_t> &lin0) {
     const int NT = pl.threads, V = pl.kp.vol;
     int64_t total = 0;
     for (int k = 0; k < pl.ept; ++k)
         for (int h = 0; h < NT / 16; ++h) {
-            uint32_t rd[16], wr[16];
-            int nw = 0;
+            int cr[16] = {0}, cw[16] = {0}, wr = 0, ww = 0;
             for (int t = 0; t < 16; ++t) {
                 const uint32_t n = (uint32_t)(k * NT + h * 16 + t);
-                if (n >= (uint32_t)V) continue;
-                uint32_t e;
-                int32_t lin;
-                spg_tma_slot(pl.kp, tp, n, e, lin);
-                rd[nw] = (uint32_t)lin;
-                wr[nw] = e;
-                ++nw;
-            }
-            for (const uint32_t *w : {rd, wr}) {
-                int cnt[16] = {0}, worst = 0;
-                for (int a = 0; a < nw; ++a) {
-                    bool dup = false;
-                    for (int b = 0; b < a; ++b) dup = dup || w[b] == w[a];
-                    if (!dup) worst = std::max(worst, ++cnt[w[a] & 15u]);
+                if (n >= (uint32_t)V) break;
+                uint32_t e = n;
+                if (tp.sk_mul) {
+                    const uint32_t lo = n % (uint32_t)tp.sk_stride;
+                    const int32_t y = (int32_t)((n / (uint32_t)tp.sk_stride) % (uint32_t)tp.sk_len);
+                    const int32_t y2 =
+                        (int32_t)((uint32_t)(y + (int32_t)(lo & 15u) * tp.sk_mul) % (uint32_t)tp.sk_len);
+                    e = (uint32_t)((int32_t)n + (y2 - y) * tp.sk_stride);
                 }
-                total += worst;
+                wr = std::max(wr, ++cr[(uint32_t)lin0[e] & 15u]);
+                ww = std::max(ww, ++cw[e & 15u]);
             }
+            total += wr + ww;
         }
     return total;
 }
@@ -249,13 +255,21 @@ static int64_t tma_permute_wavefronts(const Plan &pl, const TmaParams &tp) {
 // Pick the permute-step skew of a TMA plan: no skew, or a rotation of one
 // output dim's coordinate by (slot mod 16) * m for m in 1..3, whichever
 // takes the fewest simulated wavefronts (ties keep the simpler mapping).
+// The rotation formula is the kernel's (spg_tma_slot), written out here
+// over the precomputed table.
 int choose_skew(Plan *pl) {
     pl->sk_stride = pl->sk_len = pl->sk_mul = 0;
     if (!g_tma_skew || pl->kind != KIND_TMA || pl->kp.vol >= 65535 || pl->fo.P[pl->fo.rank - 1] == pl->fo.rank - 1)
         return SPAGHETTY_OK;   // same-order tiles: the permute step is the identity
     TmaParams tp;
     std::memset(&tp, 0, sizeof(tp));
-    int64_t best = tma_permute_wavefronts(*pl, tp);
+    std::vector<int32_t> lin0((size_t)pl->kp.vol);
+    for (uint32_t e = 0; e < (uint32_t)pl->kp.vol; ++e) {
+        int32_t a, b;
+        uint32_t pk;
+        spg_walk(pl->kp.st, e, a, b, lin0[e], pk);
+    }
+    int64_t best = tma_permute_wavefronts(*pl, tp, lin0);
     const int64_t ideal = 2 * (int64_t)((pl->kp.vol + 15) / 16);
     const BoxWalk &w = pl->kp.st;
     int32_t stride = 1;
@@ -265,7 +279,7 @@ int choose_skew(Plan *pl) {
             tp.sk_stride = stride;
             tp.sk_len = len;
             tp.sk_mul = m;
-            const int64_t wf = tma_permute_wavefronts(*pl, tp);
+            const int64_t wf = tma_permute_wavefronts(*pl, tp, lin0);
             if (wf < best) {
                 best = wf;
                 pl->sk_stride = stride;

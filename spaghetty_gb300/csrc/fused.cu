@@ -405,9 +405,15 @@ spg_fused_tma(const __grid_constant__ FusedTmaMaps maps, const __grid_constant__
     if (!ok && p.status) *(volatile int *)p.status = 1;
 }
 
+// Four load slots of 8 KB (about 48 KB per CTA, four CTAs per SM):
+// measured on GB300 on the triples groups at 16^6, 0.343-0.387 ms against
+// 0.394-0.456 ms with eight slots (two CTAs per SM); two or three slots,
+// 512 x 2 and 128 x 8 threads x elements were slower.  A t3 element's adds
+// form one dependent chain of rounded FP64 adds, so more resident warps
+// hide more of the FP64 pipe's latency.
 #define SPG_FT_NT 256
 #define SPG_FT_EPT 4
-#define SPG_FT_S 8
+#define SPG_FT_S 4
 
 // ===========================================================================
 namespace {

@@ -296,15 +296,11 @@ static int64_t smem_wavefronts(const Plan &pl, int pad, const int *e_in_of_out, 
                     if (pad) idx += idx / pad;
                     words[nw++] = idx;
                 }
+                // the words are distinct (slot -> element and the padded
+                // index are both one-to-one): count banks directly
                 int cnt[16] = {0};
                 int worst = 0;
-                for (int a = 0; a < nw; ++a) {
-                    bool dup = false;
-                    for (int b = 0; b < a; ++b) if (words[b] == words[a]) dup = true;
-                    if (dup) continue;
-                    int bank = (int)(words[a] & 15);
-                    worst = std::max(worst, ++cnt[bank]);
-                }
+                for (int a = 0; a < nw; ++a) worst = std::max(worst, ++cnt[(int)(words[a] & 15)]);
                 total += worst;
             }
     return total;
@@ -644,8 +640,11 @@ static int tma_map(const Plan &pl, const int *order, const int64_t *gstride, int
         bool merge = false;
         // a dim joins the group only where it continues the group's memory
         // range (its stride is the group's stride times the group's extent)
+        // and the group's box stays within the bulk copy's 256 per dim (a
+        // longer one would be rejected below; unmerged, the dims keep the
+        // same element order in the tile)
         if (m >= 0 && (uint64_t)gstride[d] * 8u == stride[m] * dim[m]) {
-            if (group_full) merge = true;
+            if (group_full && (int64_t)box[m] * L <= 256) merge = true;
             else if (group_unit && L == 1) merge = true;
         }
         if (merge) {
