@@ -30,6 +30,11 @@
 #define SPG_BATCH_EPT 4
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
 #define SPG_BATCH_UNIT_ELEMS 16384
+// Boxes per work unit at most: a unit's box offsets and edge limits are
+// computed once, one box per thread, into shared memory, so that the box
+// loop reads three words instead of walking the job's box grid (tens of
+// shared-memory reads of the job record per thread and box).
+#define SPG_BATCH_MAXB 64
 // Sorts of at least this many elements whose single-sort plan is the
 // TMA-staged kernel fill the GPU by themselves at a higher rate than the
 // persistent kernel: a batch launch runs each of them as its own launch,
@@ -71,19 +76,40 @@ static inline size_t batch_smem_bytes(int stage_elems) {
 // box t+S-1 in flight (SPG_BATCH_S stages of the sort's stage size) while
 // box t is written out in output order.  Every thread of the CTA calls it
 // with the same arguments; nothing is left in flight when it returns.
+// The unit's box table (shared memory, one entry per box of [b0, b1)):
+// input and output element offsets and the two edge limits.
+struct SpgBoxTab {
+    int64_t ib[SPG_BATCH_MAXB];
+    int64_t ob[SPG_BATCH_MAXB];
+    uint32_t lim[SPG_BATCH_MAXB];     // limA << 16 | limB
+};
+
+// The unit's box table, one box per thread (kept out of line: its 64-bit
+// box walk would otherwise add to the register pressure of the box loop).
+static __device__ __noinline__ void spg_batch_fill_boxes(const KParams &p, uint32_t b0, uint32_t b1,
+                                                         SpgBoxTab &bt) {
+    for (uint32_t i = threadIdx.x; b0 + i < b1; i += SPG_BATCH_NT) {
+        int64_t ib, ob;
+        uint32_t limA, limB;
+        spg_box(p, b0 + i, ib, ob, limA, limB);
+        bt.ib[i] = ib;
+        bt.ob[i] = ob;
+        bt.lim[i] = limA << 16 | limB;
+    }
+}
+
 template <int OP>
 __device__ __forceinline__ void spg_batch_tiled(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
-                                                uint32_t b0, uint32_t b1, double *sm) {
+                                                uint32_t b0, uint32_t b1, double *sm, const SpgBoxTab &bt) {
     const KParams &p = j.kp;
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(sm);
     const uint32_t stage_bytes = (uint32_t)p.stage * 8u;
     const double *in = j.in;
     auto issue = [&](uint32_t t, int st) {
         if (t < b1) {
-            int64_t ib, ob;
-            uint32_t limA, limB;
-            spg_box(p, t, ib, ob, limA, limB);
-            const double *src = in + ib;
+            const uint32_t lim = bt.lim[t - b0];
+            const uint32_t limA = lim >> 16, limB = lim & 0xFFFFu;
+            const double *src = in + bt.ib[t - b0];
             const uint32_t sb = sbase + (uint32_t)st * stage_bytes;
 #pragma unroll
             for (int k = 0; k < SPG_BATCH_EPT; ++k) {
@@ -105,10 +131,9 @@ __device__ __forceinline__ void spg_batch_tiled(const BatchJob &j, const SpgTab<
         issue(t + SPG_BATCH_S - 1, (it + SPG_BATCH_S - 1) % SPG_BATCH_S);
         spg_cp_wait<SPG_BATCH_S - 1>();        // this thread's copies for box t have landed
         __syncthreads();                       // ... and everyone else's
-        int64_t ib, ob;
-        uint32_t limA, limB;
-        spg_box(p, t, ib, ob, limA, limB);
-        double *dst = j.out + ob;
+        const uint32_t lim = bt.lim[t - b0];
+        const uint32_t limA = lim >> 16, limB = lim & 0xFFFFu;
+        double *dst = j.out + bt.ob[t - b0];
         const double *tile = sm + (size_t)st * p.stage;
         double y[SPG_BATCH_EPT];
         if (spg_reads_out<OP>::value) {
@@ -129,13 +154,37 @@ __device__ __forceinline__ void spg_batch_tiled(const BatchJob &j, const SpgTab<
     spg_cp_wait<0>();
 }
 
+// A direct sort's box from the unit's box table: every element read and
+// written by the same thread (the stride-1 index is unchanged).
+template <int OP>
+__device__ __forceinline__ void spg_batch_direct_box(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
+                                                     const SpgBoxTab &bt, uint32_t i) {
+    const uint32_t lim = bt.lim[i];
+    const uint32_t limA = lim >> 16, limB = lim & 0xFFFFu;
+    const double *src = j.in + bt.ib[i];
+    double *dst = j.out + bt.ob[i];
+    const SpgFactor fac = j.kp.fac;
+    double v[SPG_BATCH_EPT], y[SPG_BATCH_EPT];
+#pragma unroll
+    for (int k = 0; k < SPG_BATCH_EPT; ++k) {
+        v[k] = 0.0;
+        y[k] = 0.0;
+        if (spg_valid(tb.pkl[k], limA, limB)) {
+            v[k] = spg_ld_in(src + tb.ioff[k]);
+            if (spg_reads_out<OP>::value) y[k] = spg_ld_out(dst + tb.ooff[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < SPG_BATCH_EPT; ++k)
+        if (spg_valid(tb.pkl[k], limA, limB)) spg_st_out(dst + tb.ooff[k], spg_apply<OP>(v[k], y[k], fac));
+}
+
 template <int OP>
 __device__ __forceinline__ void spg_batch_units(const BatchJob &j, const SpgTab<SPG_BATCH_NT, SPG_BATCH_EPT> &tb,
-                                                uint32_t b0, uint32_t b1, double *sm) {
-    if (j.kind == KIND_TILED) spg_batch_tiled<OP>(j, tb, b0, b1, sm);
+                                                uint32_t b0, uint32_t b1, double *sm, const SpgBoxTab &bt) {
+    if (j.kind == KIND_TILED) spg_batch_tiled<OP>(j, tb, b0, b1, sm, bt);
     else
-        for (uint32_t t = b0; t < b1; ++t)
-            spg_direct_box<SPG_BATCH_NT, SPG_BATCH_EPT, OP>(j.kp, tb, j.in, j.out, t);
+        for (uint32_t t = b0; t < b1; ++t) spg_batch_direct_box<OP>(j, tb, bt, t - b0);
 }
 
 __global__ void __launch_bounds__(SPG_BATCH_NT, SPG_BATCH_MINB)
@@ -144,6 +193,7 @@ spg_batched(const BatchJob *__restrict__ jobs, uint32_t njobs,
             uint32_t *counter, int *status, int smem_elems) {
     extern __shared__ __align__(16) double sm[];
     __shared__ BatchJob sj;
+    __shared__ SpgBoxTab sbt;
     __shared__ uint32_t s_next;
     __shared__ int s_ok;
     const uint32_t tid = threadIdx.x;
@@ -175,6 +225,7 @@ spg_batched(const BatchJob *__restrict__ jobs, uint32_t njobs,
                 bool ok = (sj.kind == KIND_TILED || sj.kind == KIND_DIRECT) && sj.op >= 0 &&
                           sj.op < OP_COUNT && p.vol >= 1 && p.vol <= SPG_BATCH_VMAX &&
                           p.pad >= 0 && sj.in != nullptr && sj.out != nullptr && sj.chunk >= 1 &&
+                          sj.chunk <= SPG_BATCH_MAXB && p.lenA <= 0xFFFF && p.lenB <= 0xFFFF &&
                           p.ntiles >= 1 && p.ld.n >= 0 && p.ld.n <= SPG_MAXR && p.st.n >= 0 &&
                           p.st.n <= SPG_MAXR && p.grid.n >= 0 && p.grid.n <= SPG_MAXR &&
                           (sj.kind != KIND_TILED || (tile <= p.stage && p.stage <= smem_elems)) &&
@@ -192,16 +243,18 @@ spg_batched(const BatchJob *__restrict__ jobs, uint32_t njobs,
         if (s_ok) {
             const uint32_t b0 = (u - sj.ubeg) * sj.chunk;
             const uint32_t b1 = min(b0 + sj.chunk, sj.kp.ntiles);
+            spg_batch_fill_boxes(sj.kp, b0, b1, sbt);
+            __syncthreads();
             switch (sj.op) {
-                case OP_SORT_ONE: spg_batch_units<OP_SORT_ONE>(sj, tb, b0, b1, sm); break;
-                case OP_SORT_NEG: spg_batch_units<OP_SORT_NEG>(sj, tb, b0, b1, sm); break;
-                case OP_SORT_POW2: spg_batch_units<OP_SORT_POW2>(sj, tb, b0, b1, sm); break;
-                case OP_SORT_ANY: spg_batch_units<OP_SORT_ANY>(sj, tb, b0, b1, sm); break;
-                case OP_ACC_ONE: spg_batch_units<OP_ACC_ONE>(sj, tb, b0, b1, sm); break;
-                case OP_ACC_NEG: spg_batch_units<OP_ACC_NEG>(sj, tb, b0, b1, sm); break;
-                case OP_ACC_POW2: spg_batch_units<OP_ACC_POW2>(sj, tb, b0, b1, sm); break;
-                case OP_ACC_ANY: spg_batch_units<OP_ACC_ANY>(sj, tb, b0, b1, sm); break;
-                default: spg_batch_units<OP_GEN>(sj, tb, b0, b1, sm); break;
+                case OP_SORT_ONE: spg_batch_units<OP_SORT_ONE>(sj, tb, b0, b1, sm, sbt); break;
+                case OP_SORT_NEG: spg_batch_units<OP_SORT_NEG>(sj, tb, b0, b1, sm, sbt); break;
+                case OP_SORT_POW2: spg_batch_units<OP_SORT_POW2>(sj, tb, b0, b1, sm, sbt); break;
+                case OP_SORT_ANY: spg_batch_units<OP_SORT_ANY>(sj, tb, b0, b1, sm, sbt); break;
+                case OP_ACC_ONE: spg_batch_units<OP_ACC_ONE>(sj, tb, b0, b1, sm, sbt); break;
+                case OP_ACC_NEG: spg_batch_units<OP_ACC_NEG>(sj, tb, b0, b1, sm, sbt); break;
+                case OP_ACC_POW2: spg_batch_units<OP_ACC_POW2>(sj, tb, b0, b1, sm, sbt); break;
+                case OP_ACC_ANY: spg_batch_units<OP_ACC_ANY>(sj, tb, b0, b1, sm, sbt); break;
+                default: spg_batch_units<OP_GEN>(sj, tb, b0, b1, sm, sbt); break;
             }
         }
         __syncthreads();                      // unit done: sj and the tile may be replaced
@@ -330,7 +383,7 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         j.out = e.sorted;
         j.kind = pl.kind;
         j.op = op;
-        j.chunk = (uint32_t)std::max(1, SPG_BATCH_UNIT_ELEMS / std::max(1, (int)pl.kp.vol));
+        j.chunk = (uint32_t)std::min(SPG_BATCH_MAXB, std::max(1, SPG_BATCH_UNIT_ELEMS / std::max(1, (int)pl.kp.vol)));
         j.ubeg = (uint32_t)unit_job.size();
         const uint32_t units = (pl.kp.ntiles + j.chunk - 1) / j.chunk;
         if ((uint64_t)unit_job.size() + units > 0xFFFFFFF0ull) { rc = SPAGHETTY_ERR_OVERFLOW; break; }
@@ -624,7 +677,7 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
         j.out = e.sorted;
         j.kind = pl.kind;
         j.op = op;
-        j.chunk = (uint32_t)std::max(1, SPG_BATCH_UNIT_ELEMS / std::max(1, (int)pl.kp.vol));
+        j.chunk = (uint32_t)std::min(SPG_BATCH_MAXB, std::max(1, SPG_BATCH_UNIT_ELEMS / std::max(1, (int)pl.kp.vol)));
         j.ubeg = nunits;
         nunits += (pl.kp.ntiles + j.chunk - 1) / j.chunk;
         if (pl.kind == KIND_TILED)
