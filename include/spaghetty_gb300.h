@@ -354,7 +354,8 @@ typedef struct spaghetty_batch_entry {
 typedef struct spaghetty_batch spaghetty_batch;
 
 /* Plan every entry, cut the work into units and upload the work list (the
- * only allocation: job records, unit map, a counter and a status word).
+ * only allocations: job records, unit map, a counter and a status word, and
+ * three streams with their events when the batch has direct sorts).
  * Rejects invalid entries (SPAGHETTY_ERR_* of the first bad one; its index
  * from spaghetty_batch_bad_index()), host pointers, and any output that
  * overlaps another buffer of the batch (inputs may be shared). */
@@ -362,9 +363,14 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
 int spaghetty_batch_bad_index(void);
 
 /* Enqueue the whole batch on `stream`: the sorts of at least 2^22 elements
- * that the single-sort planner puts on the TMA-staged kernel one launch
- * each, then a counter reset and ONE persistent kernel launch over the
- * rest.  Capturable in a CUDA graph. */
+ * that the single-sort planner puts on the TMA-staged kernel ("direct"
+ * sorts) one launch each, on three streams of the batch forked from
+ * `stream` by an event, and beside them a counter reset and ONE persistent
+ * kernel launch over the rest on `stream`, which then waits for the three
+ * streams: work enqueued on `stream` afterwards sees every sort done.
+ * Capturable in a CUDA graph (the fork and join become graph edges).  Two
+ * launches of one batch must not overlap: the second waits on `stream`
+ * behind the first's join. */
 int spaghetty_batch_launch(spaghetty_batch *batch, void *stream);
 
 /* The same sorts as one launch each through spaghetty_sort_async (the plain

@@ -41,6 +41,10 @@
 // then the persistent kernel over the rest.  Both are enqueued on the same
 // stream, so a captured graph holds them all.
 #define SPG_BATCH_DIRECT_ELEMS (1 << 22)
+// Those direct launches are spread over this many streams beside the launch
+// stream: independent sorts (disjoint outputs), so one launch's last wave of
+// CTAs overlaps the next ones instead of leaving SMs idle.
+#define SPG_BATCH_AUX 3
 #ifndef SPG_BATCH_S
 #define SPG_BATCH_S 3          // cp.async stages of the tiled path
 #endif
@@ -275,6 +279,12 @@ struct spaghetty_batch {
     std::vector<BatchJob> jobs;       // host copy of the job records
     std::vector<int> direct;          // entries large enough to run as their own launch
     int64_t bytes = 0;                // algorithmic bytes of one launch
+    // streams that run the direct sorts beside the persistent kernel (forked
+    // from and joined back into the launch stream by events)
+    int naux = 0;
+    cudaStream_t aux[SPG_BATCH_AUX] = {};
+    cudaEvent_t fork = nullptr;
+    cudaEvent_t join[SPG_BATCH_AUX] = {};
 };
 
 namespace {
@@ -431,6 +441,18 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         spaghetty_batch_destroy(b);
         return SPAGHETTY_ERR_CUDA;
     }
+    if (!b->direct.empty()) {
+        // streams and events for the direct sorts; without them (creation
+        // failed) the direct sorts run in order on the launch stream
+        bool ok2 = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+        for (int a = 0; a < SPG_BATCH_AUX && ok2; ++a) {
+            ok2 = cudaStreamCreateWithFlags(&b->aux[a], cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaEventCreateWithFlags(&b->join[a], cudaEventDisableTiming) == cudaSuccess;
+            if (ok2) b->naux = a + 1;
+        }
+        if (!ok2) b->naux = 0;
+        cudaGetLastError();
+    }
     if (batch_smem_bytes(b->smem_elems) > SPG_BATCH_SMEM_OPTIN) {
         if (cudaFuncSetAttribute(spg_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)batch_smem_bytes(b->smem_elems)) != cudaSuccess) {
@@ -468,6 +490,10 @@ int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
     SpgRange range("spaghetty_batch_launch");
     if (!b) return SPAGHETTY_ERR_NULL;
     cudaStream_t st = (cudaStream_t)stream;
+    // direct sorts: forked onto the aux streams (round robin) and joined
+    // back into the launch stream before the persistent kernel
+    const bool forked = !b->direct.empty() && b->naux > 0;
+    int rc = SPAGHETTY_OK;
     if (!b->direct.empty()) {
         int cur = -1;
         if (cudaGetDevice(&cur) != cudaSuccess) cudaGetLastError();
@@ -475,17 +501,33 @@ int spaghetty_batch_launch(spaghetty_batch *b, void *stream) {
             cudaGetLastError();
             return SPAGHETTY_ERR_CUDA;
         }
-        int rc = SPAGHETTY_OK;
-        for (int i : b->direct) {
-            const spaghetty_batch_entry &e = b->entries[(size_t)i];
+        if (forked) {
+            if (cudaEventRecord(b->fork, st) != cudaSuccess) rc = SPAGHETTY_ERR_CUDA;
+            for (int a = 0; a < b->naux && !rc; ++a)
+                if (cudaStreamWaitEvent(b->aux[a], b->fork, 0) != cudaSuccess) rc = SPAGHETTY_ERR_CUDA;
+        }
+        for (size_t q = 0; q < b->direct.size() && !rc; ++q) {
+            const spaghetty_batch_entry &e = b->entries[(size_t)b->direct[q]];
             rc = spg_sort_async_on(b->dev, e.rank, e.unsorted, e.sorted, e.dims, e.perm, e.factor,
-                                   e.acc_factor, stream);
-            if (rc) break;
+                                   e.acc_factor, forked ? (void *)b->aux[q % (size_t)b->naux] : stream);
         }
         if (cur >= 0 && cur != b->dev) cudaSetDevice(cur);
-        if (rc) return rc;
     }
-    if (b->total_units == 0) return SPAGHETTY_OK;
+    // the join: every aux stream's work before anything later on the launch stream
+    auto join = [&]() {
+        if (!forked) return;
+        for (int a = 0; a < b->naux; ++a)
+            if (cudaEventRecord(b->join[a], b->aux[a]) != cudaSuccess ||
+                cudaStreamWaitEvent(st, b->join[a], 0) != cudaSuccess)
+                rc = rc ? rc : SPAGHETTY_ERR_CUDA;
+    };
+    // joined before the persistent kernel: running beside the direct sorts
+    // it was slower on the configuration mix (3587 against 3779 GB/s)
+    join();
+    if (rc || b->total_units == 0) {
+        cudaGetLastError();
+        return rc;
+    }
     if (cudaMemsetAsync(b->d_words, 0, sizeof(uint32_t), st) != cudaSuccess) {
         cudaGetLastError();
         return SPAGHETTY_ERR_CUDA;
@@ -578,6 +620,11 @@ int spaghetty_batch_destroy(spaghetty_batch *b) {
     if (b->d_jobs) cudaFree(b->d_jobs);
     if (b->d_unit_job) cudaFree(b->d_unit_job);
     if (b->d_words) cudaFree(b->d_words);
+    for (int a = 0; a < SPG_BATCH_AUX; ++a) {
+        if (b->aux[a]) cudaStreamDestroy(b->aux[a]);
+        if (b->join[a]) cudaEventDestroy(b->join[a]);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     cudaGetLastError();
     delete b;
     return SPAGHETTY_OK;
