@@ -364,13 +364,13 @@ int spaghetty_batch_bad_index(void);
 
 /* Enqueue the whole batch on `stream`: the sorts of at least 2^22 elements
  * that the single-sort planner puts on the TMA-staged kernel ("direct"
- * sorts) one launch each, on three streams of the batch forked from
- * `stream` by an event, and beside them a counter reset and ONE persistent
- * kernel launch over the rest on `stream`, which then waits for the three
- * streams: work enqueued on `stream` afterwards sees every sort done.
- * Capturable in a CUDA graph (the fork and join become graph edges).  Two
- * launches of one batch must not overlap: the second waits on `stream`
- * behind the first's join. */
+ * sorts) one launch each, spread over three streams of the batch that are
+ * forked from `stream` by an event and joined back into it; then, on
+ * `stream`, a counter reset and ONE persistent kernel launch over the rest.
+ * Work enqueued on `stream` afterwards sees every sort done.  Capturable in
+ * a CUDA graph (the fork and the join become graph edges).  Launches of one
+ * batch on different streams must not overlap (they share the counter and
+ * the three streams). */
 int spaghetty_batch_launch(spaghetty_batch *batch, void *stream);
 
 /* The same sorts as one launch each through spaghetty_sort_async (the plain
