@@ -328,6 +328,8 @@ def run_ours(args, ws, rank, local):
                 "kernel": "spg_tiled_tma, sort (16 B/element), 100^4: every perm planned on the "
                           "TMA-staged kernel, factors 1, -1, 0.5",
                 "launches": dom_n,
+                "traffic_source": "ncu capture of one launch of the 100^4 perm 4321 sort on its tuned "
+                                  "plan (profiles/tma_sort4_100.md), not of this run",
                 "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs, burst copy)"}
     breakdown = {k: round(v[1] / (v[0] / 1e3) / 1e9, 1) for k, v in per_size.items()}
     # the identity permutation at each size is a plain streaming copy (the
