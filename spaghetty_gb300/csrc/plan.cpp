@@ -195,6 +195,7 @@ int64_t largest_divisor_le(int64_t D, int64_t v) {
 }  // namespace
 
 static const int kTRun = 32;      // minimum contiguous doubles per box row
+static const int kDirectRun = 16;  // shortest shared stride-1 row of the direct kernel
 static const int kVMax = 4096;    // largest box (512 threads x 8)
 static const int kDefaultStages = 3;
 static const int kBatchThreads = 256;
@@ -342,9 +343,13 @@ int spg_plan(const Folded &fo, int op, const int *box_override, int threads_over
     pl->run_in = (int)run_len(s, L, s.in_order);
     pl->run_out = (int)run_len(s, L, s.out_order);
     // direct (no staging) only when the shared stride-1 dim alone gives
-    // coalesced rows on both sides
+    // coalesced rows on both sides: at least 16 doubles, one full 128-byte
+    // line per half warp (measured on GB300 over the 44 rank-6 perms of
+    // 16^6 that keep the stride-1 index and take no bulk tensor copy: 5815
+    // against 5403 GB/s staged through shared memory; non-cubic 5299
+    // against 4693)
     const bool same_fastest = (fo.P[R - 1] == R - 1);
-    pl->kind = (same_fastest && L[R - 1] >= kTRun) ? KIND_DIRECT : KIND_TILED;
+    pl->kind = (same_fastest && L[R - 1] >= kDirectRun) ? KIND_DIRECT : KIND_TILED;
     if (threads_override) {
         pl->threads = threads_override;
         pl->ept = ept_override;
