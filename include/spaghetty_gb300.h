@@ -234,6 +234,12 @@ const char *spaghetty_error_string(int code);
  * banks (chosen per plan by simulating them); 0 plans without the rotation.
  * Changing it drops the cached plans. */
 #define SPAGHETTY_OPT_TMA_SKEW 3
+/* SPAGHETTY_OPT_WARP_TR (default 1): transposes whose two stride-1 extents
+ * are at most 32 with a product of at most 128 move each such inner tile
+ * through one warp's registers with warp shuffles (no shared memory) when
+ * the tensor has at most 2^22 elements; 0 never, 2 at any size.  Changing it
+ * drops the cached plans. */
+#define SPAGHETTY_OPT_WARP_TR 4
 int spaghetty_set_option(int option, int value);
 
 /* Synchronise the current device and report (then clear) the kernels'
@@ -251,7 +257,9 @@ typedef struct spaghetty_plan_info {
     int kind;           /* 0 = empty, 1 = flat (rank <= 1 after folding),
                            2 = direct (fastest index unchanged),
                            3 = tiled transpose through shared memory,
-                           4 = tiled, boxes moved by TMA bulk tensor copies */
+                           4 = tiled, boxes moved by TMA bulk tensor copies,
+                           5 = small inner tiles transposed in one warp's
+                               registers with warp shuffles */
     int rank;           /* rank after dropping unit dims and fusing indices */
     int64_t dims[8];    /* folded dims, input order, last is stride-1     */
     int perm[8];        /* folded permutation, 0-based, output position -> input dim */
@@ -292,7 +300,8 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
  * threads in {128,256,512}; ept in {1,2,4,8}; stages in {0,2,3} (tiled
  * kernel: 0 = register-staged, 2/3 = cp.async pipeline depth, needs
  * ept >= 2) or 12/13/14/16 (TMA-staged kernel with 2/3/4/6 load stages;
- * threads in {128,256}, ept in {8,16}).  Pass box == NULL to clear every override.  Returns a
+ * threads in {128,256}, ept in {8,16}) or 20 (the warp-shuffle transpose:
+ * threads 256, ept = registers per lane, the problem fixes the box).  Pass box == NULL to clear every override.  Returns a
  * SPAGHETTY_* code. */
 int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op,
                        const int *box, int threads, int ept, int stages);

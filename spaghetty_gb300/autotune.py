@@ -163,6 +163,14 @@ def candidates(dims: Sequence[int], perm: Sequence[int], op: int = 0):
             for st in (12, 13, 14, 16):
                 if (bt, nt, ept, st) not in out:
                     out.append((bt, nt, ept, st))
+    # the warp-shuffle transpose (stages code 20): one tile of the two
+    # stride-1 dims per warp, when both are at most 32 long, product <= 128
+    R = len(D)
+    a, b = R - 1, P[R - 1]
+    if a != b and D[a] <= 32 and D[b] <= 32 and D[a] * D[b] <= 128:
+        wb = [1] * R
+        wb[a], wb[b] = D[a], D[b]
+        out.append((wb, 256, -(-D[a] * D[b] // 32), 20))
     return p, out
 
 
@@ -335,12 +343,12 @@ def tune(dims, perm, op=0, reps=5, cache=None, verbose=False, force=False, dump=
     if t_default < t:
         # the planner's own default beat every candidate: record it
         d = plan(dims, perm, op)
-        if d["kind"] in ("direct", "tiled", "tma"):
+        if d["kind"] in ("direct", "tiled", "tma", "warp"):
             t, box, nt, ept = t_default, d["box"], d["threads"], d["ept"]
-            st = d["stages"] + 10 if d["kind"] == "tma" else d["stages"]
+            st = d["stages"] + 10 if d["kind"] == "tma" else (20 if d["kind"] == "warp" else d["stages"])
     bpe = 16 if op == 0 else 24
-    best_tma = min((r[0] for r in results if r[1][3] >= 12), default=None)
-    best_other = min((r[0] for r in results if r[1][3] < 12), default=None)
+    best_tma = min((r[0] for r in results if 12 <= r[1][3] < 20), default=None)
+    best_other = min((r[0] for r in results if r[1][3] < 12 or r[1][3] == 20), default=None)
     ent = {"box": box, "threads": nt, "ept": ept, "stages": st, "seconds": t,
            "best_tma_gbs": n * bpe / best_tma / 1e9 if best_tma else None,
            "best_other_gbs": n * bpe / best_other / 1e9 if best_other else None,

@@ -292,6 +292,43 @@ int choose_skew(Plan *pl) {
     return SPAGHETTY_OK;
 }
 
+// SPAGHETTY_OPT_WARP_TR: 1 (default) plans the warp-shuffle transpose
+// where its rule picks it, 0 never, 2 wherever its inner tile qualifies.
+int g_warp_tr = 1;
+const int64_t kWarpMaxElems = (int64_t)1 << 22;
+
+// The warp-shuffle transpose plan (spg_warp_tr) of a folded problem: the
+// tile covers the input's and the output's stride-1 dims whole (A x B
+// elements, A, B <= 32, A*B <= 128: K = ceil(A*B/32) registers per lane),
+// one index of every other dim.  SPAGHETTY_ERR_NOKERNEL when the problem
+// does not qualify.
+int make_warp_plan(const Folded &fo, int op, double f, double g, int sms, Plan *pl) {
+    const int R = fo.rank;
+    if (fo.empty || R < 2) return SPAGHETTY_ERR_NOKERNEL;
+    const int a = R - 1, b = fo.P[R - 1];
+    if (a == b || fo.D[a] > 32 || fo.D[b] > 32 || fo.D[a] * fo.D[b] > 128) return SPAGHETTY_ERR_NOKERNEL;
+    const int V = (int)(fo.D[a] * fo.D[b]);
+    const int K = (V + 31) / 32;
+    int box[SPG_MAXR];
+    for (int d = 0; d < R; ++d) box[d] = 1;
+    box[a] = (int)fo.D[a];
+    box[b] = (int)fo.D[b];
+    Plan tp;
+    int rc = spg_plan(fo, op, box, 256, K, 0, sms, &tp);
+    if (!rc) rc = spg_build_params(&tp, f, g);
+    if (rc) return rc == SPAGHETTY_ERR_NOKERNEL ? rc : SPAGHETTY_ERR_NOKERNEL;
+    if (tp.kp.ld.n != 2 || tp.kp.st.n != 2 || tp.masked) return SPAGHETTY_ERR_NOKERNEL;
+    tp.kind = KIND_WARP;
+    tp.threads = 256;
+    tp.ept = K;
+    tp.stages = 0;
+    tp.smem_bytes = 0;
+    tp.kp.pad = 0;
+    tp.sk_stride = tp.sk_len = tp.sk_mul = 0;
+    *pl = tp;
+    return SPAGHETTY_OK;
+}
+
 int make_plan_uncached(int rank, const int *dims, const int *perm, double f, double g, int sms,
                        bool allow_tma, bool host_link, Plan *pl) {
     Folded fo;
@@ -329,6 +366,11 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
     // load stages);
     // it is ignored where the TMA kernel cannot run (misaligned or host
     // buffers), which then get the default plan
+    if (have && ov.stages == 20) {
+        // a forced warp-shuffle transpose
+        if (make_warp_plan(fo, op, f, g, sms, pl) == SPAGHETTY_OK) return SPAGHETTY_OK;
+        have = false;
+    }
     if (have && ov.stages >= 12 && !allow_tma) have = false;
     const bool want_tma = have && ov.stages >= 12;
     if (have) {
@@ -355,6 +397,15 @@ int make_plan_uncached(int rank, const int *dims, const int *perm, double f, dou
             return to_tma(pl, ov.threads, ov.ept, ov.stages - 10, true);
         }
         return SPAGHETTY_OK;
+    }
+    // small inner tiles: the warp-shuffle transpose (rule: kWarpMaxElems)
+    if (g_warp_tr) {
+        Plan wp;
+        if (make_warp_plan(fo, op, f, g, sms, &wp) == SPAGHETTY_OK &&
+            (g_warp_tr == 2 || fo.nelem <= kWarpMaxElems)) {
+            *pl = wp;
+            return SPAGHETTY_OK;
+        }
     }
     rc = spg_plan(fo, op, nullptr, 0, 0, 0, sms, pl);
     if (rc) return rc;
@@ -543,6 +594,16 @@ int launch_plan(Plan &pl, const double *u, double *s, cudaStream_t st, int dev) 
         pl.grid = (int)grid;
         void *args[] = {(void *)&mi, (void *)&mo, (void *)&pl.kp, (void *)&tl.tp};
         err = cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(block_threads(k)), args, (size_t)smem, st);
+    } else if (pl.kind == KIND_WARP) {
+        // one tile per warp at a time, eight warps per CTA
+        const SpgKernelEntry *k = find_kernel(KIND_WARP, pl.op, 256, pl.ept, 0);
+        if (!k) return SPAGHETTY_ERR_NOKERNEL;
+        const int occ = occupancy(k, 0);
+        int64_t grid = std::min<int64_t>(((int64_t)pl.kp.ntiles + 7) / 8, (int64_t)sms * occ);
+        if (grid < 1) grid = 1;
+        pl.grid = (int)grid;
+        void *args[] = {(void *)&u, (void *)&s, (void *)&pl.kp};
+        err = cudaLaunchKernel(k->fn, dim3((unsigned)grid), dim3(256), args, 0, st);
     } else {
         const SpgKernelEntry *k = find_kernel(pl.kind, pl.op, pl.threads, pl.ept, pl.stages);
         if (!k) return SPAGHETTY_ERR_NOKERNEL;
@@ -973,6 +1034,13 @@ int spaghetty_set_option(int option, int value) {
         g_pipeline = value ? 1 : 0;
         return SPAGHETTY_OK;
     }
+    if (option == SPAGHETTY_OPT_WARP_TR) {
+        if (value < 0 || value > 2) return SPAGHETTY_ERR_CONFIG;
+        std::lock_guard<std::mutex> lk(g_plans_mu);
+        g_warp_tr = value;
+        g_plans.clear();
+        return SPAGHETTY_OK;
+    }
     if (option == SPAGHETTY_OPT_TMA_SKEW) {
         std::lock_guard<std::mutex> lk(g_plans_mu);
         g_tma_skew = value ? 1 : 0;
@@ -1169,8 +1237,11 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
     std::vector<int64_t> got((size_t)n, -1);
     // one staging tile: the whole buffer of the register-staged kernel, one
     // stage of the pipelined kernel
-    const int64_t smem_elems = pl.stages ? (int64_t)kp.stage
-                                         : pl.smem_bytes / (int64_t)sizeof(double);
+    // (the warp-shuffle transpose's "tile" is the warp's registers, vol
+    // elements in input order, with no padding)
+    const int64_t smem_elems = pl.kind == KIND_WARP ? (int64_t)kp.vol
+                               : pl.stages ? (int64_t)kp.stage
+                                           : pl.smem_bytes / (int64_t)sizeof(double);
     if (pl.stages && (int64_t)pl.stages * kp.stage * 8 > pl.smem_bytes) return SPAGHETTY_ERR_CONFIG;
     std::vector<int64_t> sm((size_t)std::max<int64_t>(smem_elems, 1), -2);
     int64_t reads = 0, writes = 0;
@@ -1203,7 +1274,7 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
                 }
             }
         }
-        if (pl.kind == KIND_TILED) {
+        if (pl.kind == KIND_TILED || pl.kind == KIND_WARP) {
             for (uint32_t e = 0; e < (uint32_t)kp.vol; ++e) {
                 int32_t a, b, lin;
                 uint32_t pk;
@@ -1255,6 +1326,25 @@ int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const
     if (rc) return rc;
     if (fo.empty || fo.rank < 2) return SPAGHETTY_ERR_CONFIG;
     const bool tma = stages == 12 || stages == 13 || stages == 14 || stages == 16;
+    if (stages == 20) {
+        // the warp-shuffle transpose: its box is fixed by the problem
+        Plan wp;
+        const int opw = op == 0 ? OP_SORT_ANY : (op == 1 ? OP_ACC_ANY : OP_GEN);
+        if (threads != 256 || make_warp_plan(fo, opw, 0.5, 1.0, 152, &wp) != SPAGHETTY_OK || wp.ept != ept)
+            return SPAGHETTY_ERR_CONFIG;
+        TuneOverride ov;
+        for (int d = 0; d < SPG_MAXR; ++d) ov.box[d] = d < fo.rank ? wp.box[d] : 1;
+        ov.threads = 256;
+        ov.ept = ept;
+        ov.stages = 20;
+        {
+            std::lock_guard<std::mutex> lk(g_mu);
+            g_tune[tune_key(fo, opw)] = ov;
+        }
+        std::lock_guard<std::mutex> lk2(g_plans_mu);
+        g_plans.clear();
+        return SPAGHETTY_OK;
+    }
     if (tma) {
         if ((threads != 128 && threads != 256) || (ept != 8 && ept != 16)) return SPAGHETTY_ERR_CONFIG;
     } else {

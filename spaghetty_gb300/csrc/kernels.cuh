@@ -563,6 +563,75 @@ spg_flat(const double *__restrict__ in, double *__restrict__ out, int64_t n,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Warp-shuffle transpose of small inner tiles.  When the input's stride-1
+// dim a and the output's stride-1 dim b are different and short (A, B <= 32,
+// A*B <= 32*K), one warp moves a whole A x B tile (every other dim is a
+// single index of the tile grid) through its registers: it loads the tile
+// in input order (lane l holds elements l, l+32, ... : rows of A contiguous
+// doubles), and each lane fetches the elements of its output-order slots
+// from the lanes that hold them with warp shuffles (K shuffles of 64 bits
+// per slot, keeping the one from the right register), then stores them in
+// output order (rows of B contiguous doubles).  No shared memory and no
+// block barrier: a warp's tile is done after one round of loads, shuffles
+// and stores, which is what small tensors (where a few microseconds of
+// latency per staged box dominate) and batches of small tiles need.  The
+// per-slot offsets come from the plan's two box walks (ld: a then b; st:
+// b then a), whose lin index is the element's input-order place in the tile.
+template <int OP, int K>
+__global__ void __launch_bounds__(256)
+spg_warp_tr(const double *__restrict__ in, double *__restrict__ out, const __grid_constant__ KParams p) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t V = (uint32_t)p.vol;
+    int32_t ioff[K], ooff[K];
+    uint32_t sl[K], sr[K];          // output slot m: source lane and register
+    bool vin[K], vout[K];
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+        const uint32_t e = lane + 32u * (uint32_t)j;
+        int32_t a, b, lin;
+        uint32_t pk;
+        vin[j] = e < V;
+        vout[j] = e < V;
+        ioff[j] = 0;
+        ooff[j] = 0;
+        sl[j] = 0;
+        sr[j] = 0;
+        if (e < V) {
+            spg_walk(p.ld, e, a, b, lin, pk);
+            ioff[j] = a;
+            spg_walk(p.st, e, a, b, lin, pk);
+            ooff[j] = a;
+            sl[j] = (uint32_t)lin & 31u;
+            sr[j] = (uint32_t)lin >> 5;
+        }
+    }
+    const SpgFactor fac = p.fac;
+    for (uint32_t t = warp; t < p.ntiles; t += nwarps) {
+        int64_t ib, ob;
+        uint32_t limA, limB;
+        spg_box(p, t, ib, ob, limA, limB);
+        double v[K], y[K];
+#pragma unroll
+        for (int j = 0; j < K; ++j) {
+            v[j] = vin[j] ? spg_ld_in(in + ib + ioff[j]) : 0.0;
+            y[j] = (spg_reads_out<OP>::value && vout[j]) ? spg_ld_out(out + ob + ooff[j]) : 0.0;
+        }
+#pragma unroll
+        for (int m = 0; m < K; ++m) {
+            double r = 0.0;
+#pragma unroll
+            for (int j = 0; j < K; ++j) {
+                const double x = __shfl_sync(0xffffffffu, v[j], (int)sl[m]);
+                if (sr[m] == (uint32_t)j) r = x;
+            }
+            if (vout[m]) spg_st_out(out + ob + ooff[m], spg_apply<OP>(r, y[m], fac));
+        }
+    }
+}
+
 // Table entry emitted by the generator for every compiled variant.
 struct SpgKernelEntry {
     int kind;       // SpgKind

@@ -91,7 +91,9 @@ struct KParams {
     SpgFactor fac;
 };
 
-enum SpgKind { KIND_EMPTY = 0, KIND_FLAT = 1, KIND_DIRECT = 2, KIND_TILED = 3, KIND_TMA = 4 };
+// KIND_WARP: the warp-shuffle transpose (spg_warp_tr) of small inner tiles,
+// both stride-1 extents at most 32 and their product at most 128.
+enum SpgKind { KIND_EMPTY = 0, KIND_FLAT = 1, KIND_DIRECT = 2, KIND_TILED = 3, KIND_TMA = 4, KIND_WARP = 5 };
 
 // TMA-staged kernel: how box t's tile coordinates map onto the two 5-D
 // tensor maps (input map over the folded input dims in input order, output

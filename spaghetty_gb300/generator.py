@@ -30,6 +30,7 @@ HEADER = """// GENERATED by spaghetty_gb300/generator.py -- do not edit.
 TMA_THREADS = (128, 256)
 TMA_EPTS = (8, 16)
 TMA_STAGES = (2, 3, 4, 6)
+WARP_KS = (1, 2, 3, 4)     # warp-shuffle transpose: registers per lane (tile <= 32*K)
 
 
 STAGES = (2, 3)
@@ -55,6 +56,8 @@ def variants(op: int):
             for st in TMA_STAGES:
                 out.append(("KIND_TMA", nt, ept, st,
                             "spg_tiled_tma<%d, %d, %s, %d>" % (nt, ept, OPS[op], st)))
+    for k in WARP_KS:
+        out.append(("KIND_WARP", 256, k, 0, "spg_warp_tr<%s, %d>" % (OPS[op], k)))
     return out
 
 

@@ -159,7 +159,7 @@ def plan(dims: Sequence[int], perm: Sequence[int], op: int = 0):
     check(rc, "plan")
     r = info.rank
     return {
-        "kind": ("empty", "flat", "direct", "tiled", "tma")[info.kind],
+        "kind": ("empty", "flat", "direct", "tiled", "tma", "warp")[info.kind],
         "rank": r,
         "dims": [int(info.dims[q]) for q in range(r)],
         "perm": [int(info.perm[q]) for q in range(r)],

@@ -68,8 +68,10 @@ def verify(dims, perm, op=0, sms=152):
 def test_folding(dims, perm, rank, kind):
     p = plan(dims, perm)
     # tiled and direct plans run on the TMA-staged kernel when its boxes
-    # allow it (direct ones with the same-order layout)
-    assert p["rank"] == rank and (p["kind"] == kind or (kind in ("tiled", "direct") and p["kind"] == "tma"))
+    # allow it (direct ones with the same-order layout); small transposes
+    # (both stride-1 extents <= 32, product <= 128) on the warp-shuffle kernel
+    assert p["rank"] == rank and (p["kind"] == kind or (kind in ("tiled", "direct") and p["kind"] == "tma")
+                                  or (kind == "tiled" and p["kind"] == "warp"))
     assert int(np.prod(p["dims"])) == int(np.prod(dims))
 
 
