@@ -128,17 +128,17 @@ __device__ __forceinline__ void spg_batch_tiled(const BatchJob &j, const SpgTab<
     const SpgFactor fac = p.fac;
 #pragma unroll
     for (int q = 0; q < SPG_BATCH_S - 1; ++q) issue(b0 + (uint32_t)q, q);
+    // One block barrier per box: after it every thread's copies of box t
+    // have landed and every thread has finished box t-1, whose stage is the
+    // one refilled (with box t+S-1) right after it.
     int it = 0;
     for (uint32_t t = b0; t < b1; ++t, ++it) {
         const int st = it % SPG_BATCH_S;
-        __syncthreads();                       // the stage refilled below is no longer read
-        issue(t + SPG_BATCH_S - 1, (it + SPG_BATCH_S - 1) % SPG_BATCH_S);
-        spg_cp_wait<SPG_BATCH_S - 1>();        // this thread's copies for box t have landed
-        __syncthreads();                       // ... and everyone else's
         const uint32_t lim = bt.lim[t - b0];
         const uint32_t limA = lim >> 16, limB = lim & 0xFFFFu;
         double *dst = j.out + bt.ob[t - b0];
-        const double *tile = sm + (size_t)st * p.stage;
+        // a sortacc's old output: loads issued before the wait, which
+        // hides their latency
         double y[SPG_BATCH_EPT];
         if (spg_reads_out<OP>::value) {
 #pragma unroll
@@ -147,6 +147,10 @@ __device__ __forceinline__ void spg_batch_tiled(const BatchJob &j, const SpgTab<
                 if (spg_valid(tb.pks[k], limA, limB)) y[k] = spg_ld_out(dst + tb.ooff[k]);
             }
         }
+        spg_cp_wait<SPG_BATCH_S - 2>();        // this thread's copies for box t have landed
+        __syncthreads();                       // ... everyone's, and box t-1 is done
+        issue(t + SPG_BATCH_S - 1, (it + SPG_BATCH_S - 1) % SPG_BATCH_S);
+        const double *tile = sm + (size_t)st * p.stage;
 #pragma unroll
         for (int k = 0; k < SPG_BATCH_EPT; ++k) {
             if (spg_valid(tb.pks[k], limA, limB)) {

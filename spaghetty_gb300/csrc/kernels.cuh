@@ -466,17 +466,17 @@ spg_tiled_async(const double *__restrict__ in, double *__restrict__ out,
     uint32_t t = blockIdx.x;
 #pragma unroll
     for (int q = 0; q < S - 1; ++q) issue(t + (uint32_t)q * G, q);
+    // One block barrier per box: after it every thread's copies of box t
+    // have landed and every thread has finished box t-1, whose stage is the
+    // one refilled (with box t+S-1) right after it.  A sortacc's old-output
+    // loads go out before the wait, which hides their latency (over the
+    // host link, for host-mapped buffers, a few microseconds).
     for (int it = 0; t < p.ntiles; t += G, ++it) {
         const int st = it % S;
-        __syncthreads();                       // the stage refilled below is no longer read
-        issue(t + (uint32_t)(S - 1) * G, (it + S - 1) % S);
-        spg_cp_wait<S - 1>();                  // this thread's copies for box t have landed
-        __syncthreads();                       // ... and everyone else's
         int64_t ib, ob;
         uint32_t limA, limB;
         spg_box(p, t, ib, ob, limA, limB);
         double *dst = out + ob;
-        const double *tile = sm + st * p.stage;
         double y[EPT];
         if (spg_reads_out<OP>::value) {
 #pragma unroll
@@ -485,6 +485,10 @@ spg_tiled_async(const double *__restrict__ in, double *__restrict__ out,
                 if (spg_valid(tb.pks[k], limA, limB)) y[k] = spg_ld_out(dst + tb.ooff[k]);
             }
         }
+        spg_cp_wait<S - 2>();                  // this thread's copies for box t have landed
+        __syncthreads();                       // ... everyone's, and box t-1 is done
+        issue(t + (uint32_t)(S - 1) * G, (it + S - 1) % S);
+        const double *tile = sm + st * p.stage;
         spg_write_box<NT, EPT, OP>(tb, tile, y, dst, limA, limB, fac);
     }
     spg_cp_wait<0>();
