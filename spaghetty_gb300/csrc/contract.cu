@@ -156,12 +156,42 @@ spg_contract(const __grid_constant__ ContractParams p) {
                 for (int i = 0; i < RM; ++i) av[i] = As[buf][kk][RM * tx + i];
 #pragma unroll
                 for (int j = 0; j < RN; ++j) bv[j] = Bs[buf][kk][RN * ty + j];
+                if (FMA) {
 #pragma unroll
-                for (int i = 0; i < RM; ++i)
+                    for (int i = 0; i < RM; ++i)
 #pragma unroll
-                    for (int j = 0; j < RN; ++j)
-                        acc[i][j] = FMA ? __fma_rn(av[i], bv[j], acc[i][j])
-                                        : __dadd_rn(acc[i][j], __dmul_rn(av[i], bv[j]));
+                        for (int j = 0; j < RN; ++j) acc[i][j] = __fma_rn(av[i], bv[j], acc[i][j]);
+                } else {
+                    // exact mode: every product rounded, then added in k
+                    // order.  The products take the integer multiply
+                    // (spg_mul_int: the same bits as __dmul_rn wherever it
+                    // applies), which leaves the FP64 pipe only the adds;
+                    // one warp vote per k step sends a warp with any product
+                    // it does not cover to the rounded multiply.
+                    SpgFactor bf[RN];
+#pragma unroll
+                    for (int j = 0; j < RN; ++j) bf[j] = spg_mul_operand(bv[j]);
+                    double pr[RM][RN];
+                    bool exact = true;
+#pragma unroll
+                    for (int i = 0; i < RM; ++i)
+#pragma unroll
+                        for (int j = 0; j < RN; ++j) pr[i][j] = spg_mul_int(av[i], bf[j], exact);
+                    if (!__all_sync(0xffffffffu, exact)) {
+                        // out of line (spg_dmul_branch): inlined, the
+                        // compiler predicates these multiplies into every
+                        // step, where they occupy the FP64 pipe even when
+                        // predicated off (0.85 ms against 0.49 ms at 24^6)
+#pragma unroll
+                        for (int i = 0; i < RM; ++i)
+#pragma unroll
+                            for (int j = 0; j < RN; ++j) pr[i][j] = spg_dmul_branch(av[i], bv[j]);
+                    }
+#pragma unroll
+                    for (int i = 0; i < RM; ++i)
+#pragma unroll
+                        for (int j = 0; j < RN; ++j) acc[i][j] = __dadd_rn(acc[i][j], pr[i][j]);
+                }
             }
             __syncthreads();                // buffer buf is refilled two steps on
         }

@@ -127,7 +127,29 @@ __device__ __forceinline__ double spg_mul_int(double x, const SpgFactor &F, bool
     const bool zero = ((hi & 0x7FFFFFFFu) | lo) == 0u;
     const bool normal = ex - 1u < 2046u && e - 1u < 2046u;
     exact = exact && F.mul_ok != 0u && (normal || zero);
-    return zero ? __hiloint2double((int)sign, 0) : __hiloint2double((int)(rhi | sign), (int)rlo);
+    // select on the 32-bit halves: a select of two doubles would be an FP64
+    // pipe instruction on GB300
+    return __hiloint2double((int)(zero ? sign : (rhi | sign)), (int)(zero ? 0u : rlo));
+}
+
+// The integer multiply's operand fields of a run-time factor f (the host
+// builds them once per call with spg_make_factor; the fused contraction's
+// products have a different factor every step).
+__device__ __forceinline__ SpgFactor spg_mul_operand(double f) {
+    SpgFactor F;
+    const uint32_t hi = (uint32_t)__double2hiint(f);
+    const uint32_t ef = (hi >> 20) & 0x7FFu;
+    F.f = f;
+    F.g = 0.0;
+    F.k = 0;
+    F.elo = 0;
+    F.erange = 0;
+    F.sgn_hi = hi & 0x80000000u;
+    F.mhi = (hi & 0xFFFFFu) | 0x100000u;
+    F.mlo = (uint32_t)__double2loint(f);
+    F.ebias = (int32_t)ef - 1023;
+    F.mul_ok = (ef - 1u < 2046u) ? 1u : 0u;
+    return F;
 }
 
 __device__ __forceinline__ double spg_mul(double x, const SpgFactor &F) {
