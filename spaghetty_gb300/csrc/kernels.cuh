@@ -209,10 +209,12 @@ __device__ __forceinline__ double spg_apply_fast(double x, double y, const SpgFa
     return spg_apply<OP>(x, y, F);
 }
 
+// (the multiply out of line: this runs only for a warp with an inexact
+// element, and inlined the compiler predicates it into every box)
 template <int OP>
 __device__ __forceinline__ double spg_apply_mul(double x, double y, const SpgFactor &F) {
-    if (OP == OP_SORT_POW2) return __dmul_rn(x, F.f);
-    if (OP == OP_ACC_POW2) return __dadd_rn(y, __dmul_rn(x, F.f));
+    if (OP == OP_SORT_POW2) return spg_dmul_branch(x, F.f);
+    if (OP == OP_ACC_POW2) return __dadd_rn(y, spg_dmul_branch(x, F.f));
     return spg_apply<OP>(x, y, F);
 }
 
