@@ -34,6 +34,9 @@ EPTS = (1, 2, 4, 8)
 TMA_THREADS = (128, 256)
 TMA_EPTS = (8, 16)
 VMAX = 4096
+# run targets (contiguous doubles per box row) of the candidate boxes; 24, 40
+# and 48 reach boxes that split a 100-long side in halves or thirds
+RUNS = (16, 24, 32, 40, 48, 64)
 
 
 def _split_len(D: int, want: int) -> int:
@@ -125,7 +128,7 @@ def candidates(dims: Sequence[int], perm: Sequence[int], op: int = 0):
         return p, []
     D, P = p["dims"], p["perm"]
     boxes = []
-    for ti, to, vt in itertools.product((16, 32, 64), (16, 32, 64), (512, 1024, 2048, 4096)):
+    for ti, to, vt in itertools.product(RUNS, RUNS, (512, 1024, 2048, 4096)):
         b = greedy_box(D, P, ti, to, vt)
         if b not in boxes:
             boxes.append(b)
