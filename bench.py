@@ -289,14 +289,27 @@ def run_ours(args, ws, rank, local):
     # e2e: same sweep through the C ABI with pinned host buffers (the kernels
     # read and write them in place); the staged variant for comparison
     e2e = None
-    if rank == 0 and not args.no_e2e:
+    if not args.no_e2e:
+        # every rank runs the e2e sweep on its own GPU and host buffers; the
+        # whole-job value is all ranks' bytes over the slowest rank's time
         e2e = run_e2e(args, cases, torch, L, int_array, ctypes, warm=max(3, args.warmup))
-        # the two alternatives, for comparison only: one warm-up sweep each
+        nbytes, secs = e2e.pop("_bytes"), e2e.pop("_seconds")
+        if ws > 1:
+            t = torch.tensor([secs], dtype=torch.float64)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            e2e["value"] = round(nbytes * ws / float(t[0]) / 1e9, 2)
+            e2e["h2d_bytes_per_step"] *= ws
+            e2e["d2h_bytes_per_step"] *= ws
+    if rank == 0 and not args.no_e2e:
+        # the two alternatives, for comparison only (rank 0): one warm-up sweep each
         L.spaghetty_set_option(1, 0)
         staged = run_e2e(args, cases, torch, L, int_array, ctypes, warm=1)
         L.spaghetty_set_option(1, 1)
         L.spaghetty_set_option(2, 1)
         piped = run_e2e(args, cases, torch, L, int_array, ctypes, warm=1)
+        for alt in (staged, piped):
+            alt.pop("_bytes")
+            alt.pop("_seconds")
         L.spaghetty_set_option(2, 0)
         e2e["staged_copies_value"] = staged["value"]
         e2e["pipelined_slabs_value"] = piped["value"]
@@ -407,7 +420,7 @@ def run_e2e(args, cases, torch, L, int_array, ctypes, warm=3):
             d2h += n * 8
             total_b += case_bytes(dims, acc)
     dt = time.perf_counter() - t0
-    return {"value": round(total_b / dt / 1e9, 2), "unit": UNIT,
+    return {"value": round(total_b / dt / 1e9, 2), "unit": UNIT, "_bytes": total_b, "_seconds": dt,
             "h2d_bytes_per_step": h2d // steps, "d2h_bytes_per_step": d2h // steps,
             "steps": steps, "warmup_sweeps": warm,
             "how": "tce_sort_4/tce_sortacc_4 C-ABI calls on pinned host "
@@ -563,8 +576,45 @@ def cpu_baseline(budget_s):
     if r is None:
         return {"value": None, "unit": UNIT, "error": "reference nests unavailable"}
     v, cores, desc, _ = r
-    return {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": "reference",
-            "sample": desc}
+    out = {"value": round(v, 2), "unit": UNIT, "cores": cores, "kind": "reference",
+           "sample": desc}
+    try:
+        out["old_sort"] = old_sort_sample(min(8.0, budget_s / 2))
+    except Exception as e:  # noqa: BLE001
+        out["old_sort"] = {"value": None, "error": str(e)[:200]}
+    return out
+
+
+def old_sort_sample(budget_s):
+    """The Hirata routines themselves (trunk/old_sort.f: old_sort_4 /
+    old_sortacc_4, restated in C by the oracle, one host thread as the Fortran
+    is serial), timed on the same interleaved sample of the sweep for a
+    bounded time: the code NWChem runs when it does not link a tuned
+    library."""
+    import numpy as np
+    from oracle import oracle as O
+    from spaghetty_gb300.workloads import PERMS4, SORT4_DIMS
+    rng = np.random.default_rng(5)
+    bufs = {}
+    for dims in SORT4_DIMS:
+        m = int(np.prod(dims))
+        bufs[dims] = (rng.uniform(-1, 1, m), rng.uniform(-1, 1, m))
+    cases = [(d, p, f, a) for p in PERMS4 for f in (1.0, -1.0, 0.5) for a in (False, True)
+             for d in SORT4_DIMS]
+    tb, tt, k = 0, 0.0, 0
+    t_end = time.perf_counter() + budget_s
+    while time.perf_counter() < t_end and k < len(cases):
+        dims, perm, f, acc = cases[k]
+        u, y = bufs[dims]
+        t0 = time.perf_counter()
+        O.old_sort(u, dims, perm, f, out=y, acc=acc)
+        tt += time.perf_counter() - t0
+        tb += u.size * (24 if acc else 16)
+        k += 1
+    return {"value": round(tb / tt / 1e9, 2) if tt else None, "unit": UNIT, "cores": 1,
+            "sample": "old_sort_4 / old_sortacc_4 (trunk/old_sort.f:33-95,512-575, the oracle's C "
+                      "restatement, -O2 -ffp-contract=off), %d calls of the sweep, sizes interleaved"
+                      % k}
 
 
 def run_reference(args, ws, rank):
@@ -1003,6 +1053,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("gloo", init_method="env://")
     line = run_ours(args, ws, rank, local)
+    if ws > 1:
+        torch.distributed.barrier()        # rank 0's extra sections are done too
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:

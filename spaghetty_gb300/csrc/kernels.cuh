@@ -615,14 +615,13 @@ spg_warp_tr(const double *__restrict__ in, double *__restrict__ out, const __gri
     const uint32_t V = (uint32_t)p.vol;
     int32_t ioff[K], ooff[K];
     uint32_t sl[K], sr[K];          // output slot m: source lane and register
-    bool vin[K], vout[K];
+    bool valid[K];                  // slot j of the lane holds an element (input and output order alike)
 #pragma unroll
     for (int j = 0; j < K; ++j) {
         const uint32_t e = lane + 32u * (uint32_t)j;
         int32_t a, b, lin;
         uint32_t pk;
-        vin[j] = e < V;
-        vout[j] = e < V;
+        valid[j] = e < V;
         ioff[j] = 0;
         ooff[j] = 0;
         sl[j] = 0;
@@ -644,8 +643,8 @@ spg_warp_tr(const double *__restrict__ in, double *__restrict__ out, const __gri
         double v[K], y[K];
 #pragma unroll
         for (int j = 0; j < K; ++j) {
-            v[j] = vin[j] ? spg_ld_in(in + ib + ioff[j]) : 0.0;
-            y[j] = (spg_reads_out<OP>::value && vout[j]) ? spg_ld_out(out + ob + ooff[j]) : 0.0;
+            v[j] = valid[j] ? spg_ld_in(in + ib + ioff[j]) : 0.0;
+            y[j] = (spg_reads_out<OP>::value && valid[j]) ? spg_ld_out(out + ob + ooff[j]) : 0.0;
         }
 #pragma unroll
         for (int m = 0; m < K; ++m) {
@@ -655,7 +654,7 @@ spg_warp_tr(const double *__restrict__ in, double *__restrict__ out, const __gri
                 const double x = __shfl_sync(0xffffffffu, v[j], (int)sl[m]);
                 if (sr[m] == (uint32_t)j) r = x;
             }
-            if (vout[m]) spg_st_out(out + ob + ooff[m], spg_apply<OP>(r, y[m], fac));
+            if (valid[m]) spg_st_out(out + ob + ooff[m], spg_apply<OP>(r, y[m], fac));
         }
     }
 }
