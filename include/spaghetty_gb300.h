@@ -240,6 +240,17 @@ const char *spaghetty_error_string(int code);
  * the tensor has at most 2^22 elements; 0 never, 2 at any size.  Changing it
  * drops the cached plans. */
 #define SPAGHETTY_OPT_WARP_TR 4
+/* SPAGHETTY_OPT_BATCH_OWN_MIN (default 16777216 = 2^24): batches created
+ * afterwards run every sort of at least this many elements that
+ * SPAGHETTY_OPT_BATCH_OWN_KINDS admits as its own launch (on streams forked
+ * from the launch stream and joined before the persistent kernel) instead
+ * of on the persistent kernel's work list; 0 keeps every sort on the work
+ * list. */
+#define SPAGHETTY_OPT_BATCH_OWN_MIN 5
+/* SPAGHETTY_OPT_BATCH_OWN_KINDS (default 0): which of those large sorts
+ * leave the work list: 0 = those whose single-sort plan is the TMA-staged
+ * kernel, 1 = all of them. */
+#define SPAGHETTY_OPT_BATCH_OWN_KINDS 6
 int spaghetty_set_option(int option, int value);
 
 /* Synchronise the current device and report (then clear) the kernels'
@@ -371,9 +382,10 @@ typedef struct spaghetty_batch spaghetty_batch;
 int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghetty_batch **out);
 int spaghetty_batch_bad_index(void);
 
-/* Enqueue the whole batch on `stream`: the sorts of at least 2^22 elements
- * that the single-sort planner puts on the TMA-staged kernel ("direct"
- * sorts) one launch each, spread over three streams of the batch that are
+/* Enqueue the whole batch on `stream`: the sorts of at least
+ * SPAGHETTY_OPT_BATCH_OWN_MIN elements (2^24 by default) that the
+ * single-sort planner puts on the TMA-staged kernel ("direct" sorts; the
+ * options in force when the batch was created) one launch each, spread over three streams of the batch that are
  * forked from `stream` by an event and joined back into it; then, on
  * `stream`, a counter reset and ONE persistent kernel launch over the rest.
  * Work enqueued on `stream` afterwards sees every sort done.  Capturable in
@@ -485,8 +497,9 @@ int ccsd_t2_8_status(const double *a_raw, const int *size_a, const double *b_raw
  * loads it holds that array until exit); the caller passes only inputs and
  * outputs, and the call allocates nothing.  Limits: at most 1024 sorts, and
  * the work list must fit the 4 MiB: 896 bytes per sort plus 4 bytes per work
- * unit of ~16K elements (with 1024 sorts, about 819,000 units, i.e. some
- * 13 G elements); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The first
+ * unit, a unit being up to 64 boxes and 64K elements of one sort (with 1024
+ * sorts, about 819,000 units: some 53 G elements on 1024-element boxes, 13 G
+ * on 256-element boxes); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The first
  * call on a device looks up the array's device address (set-up); make that
  * first call before any stream capture.  Every call shares the one array,
  * which keeps the previous call's contents: the counter and status word are

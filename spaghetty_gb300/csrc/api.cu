@@ -1047,6 +1047,8 @@ int spaghetty_set_option(int option, int value) {
         g_plans.clear();
         return SPAGHETTY_OK;
     }
+    if (option == SPAGHETTY_OPT_BATCH_OWN_MIN || option == SPAGHETTY_OPT_BATCH_OWN_KINDS)
+        return spg_batch_option(option, value);
     return SPAGHETTY_ERR_CONFIG;
 }
 

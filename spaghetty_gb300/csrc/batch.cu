@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstring>
 #include <mutex>
@@ -29,18 +30,33 @@
 #define SPG_BATCH_NT 256
 #define SPG_BATCH_EPT 4
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
-#define SPG_BATCH_UNIT_ELEMS 16384
+// Elements per work unit (consecutive boxes of one sort, at most
+// SPG_BATCH_MAXB of them).  Each unit starts and drains its own cp.async
+// pipeline, so longer units leave fewer bubbles: on the batched
+// configuration's mix 16K -> 64K elements went from 4070 to 4235 GB/s (all
+// sorts on the work list); 48K and 96K measured 4218 and 4133.
+#ifndef SPG_BATCH_UNIT_ELEMS
+#define SPG_BATCH_UNIT_ELEMS 65536
+#endif
 // Boxes per work unit at most: a unit's box offsets and edge limits are
 // computed once, one box per thread, into shared memory, so that the box
 // loop reads three words instead of walking the job's box grid (tens of
 // shared-memory reads of the job record per thread and box).
+#ifndef SPG_BATCH_MAXB
 #define SPG_BATCH_MAXB 64
+#endif
 // Sorts of at least this many elements whose single-sort plan is the
 // TMA-staged kernel fill the GPU by themselves at a higher rate than the
 // persistent kernel: a batch launch runs each of them as its own launch,
 // then the persistent kernel over the rest.  Both are enqueued on the same
-// stream, so a captured graph holds them all.
-#define SPG_BATCH_DIRECT_ELEMS (1 << 22)
+// stream, so a captured graph holds them all.  On the batched
+// configuration's mix (random 6-D shapes, random factors) the persistent
+// kernel moves the sorts of 2^22..2^24 elements as fast as their own
+// launches do, and the threshold 2^24 measured best (GB/s with 64K-element
+// units: 2^22 4193, 2^23 4256, 2^24 4269, none 4235).
+// SPAGHETTY_OPT_BATCH_OWN_MIN and SPAGHETTY_OPT_BATCH_OWN_KINDS change the
+// size and the plan kinds.
+#define SPG_BATCH_DIRECT_ELEMS (1 << 24)
 // Those direct launches are spread over this many streams beside the launch
 // stream: independent sorts (disjoint outputs), so one launch's last wave of
 // CTAs overlaps the next ones instead of leaving SMs idle.
@@ -294,6 +310,12 @@ struct spaghetty_batch {
 namespace {
 thread_local int g_batch_bad_index = -1;
 
+// Which sorts leave the work list for their own launches (read when a batch
+// is created): at least g_own_min elements (0: none), and, unless
+// g_own_any, only those whose single-sort plan is the TMA-staged kernel.
+std::atomic<int64_t> g_own_min{SPG_BATCH_DIRECT_ELEMS};
+std::atomic<int> g_own_any{0};
+
 // Tuned tile-shape rules, one per size bucket (spaghetty_batch_tune_set).
 std::mutex g_rules_mu;
 std::vector<SpgBatchRule> g_rules;
@@ -339,6 +361,20 @@ int grid_for(spaghetty_batch *b) {
 }
 }  // namespace
 
+int spg_batch_option(int option, int value) {
+    if (option == SPAGHETTY_OPT_BATCH_OWN_MIN) {
+        if (value < 0) return SPAGHETTY_ERR_CONFIG;
+        g_own_min.store(value);
+        return SPAGHETTY_OK;
+    }
+    if (option == SPAGHETTY_OPT_BATCH_OWN_KINDS) {
+        if (value < 0 || value > 1) return SPAGHETTY_ERR_CONFIG;
+        g_own_any.store(value);
+        return SPAGHETTY_OK;
+    }
+    return SPAGHETTY_ERR_CONFIG;
+}
+
 extern "C" {
 
 int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghetty_batch **out) {
@@ -376,8 +412,10 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         const uintptr_t nb = (uintptr_t)fo.nelem * sizeof(double);
         ranges.push_back({(uintptr_t)e.unsorted, (uintptr_t)e.unsorted + nb, i, false});
         ranges.push_back({(uintptr_t)e.sorted, (uintptr_t)e.sorted + nb, i, true});
-        if (fo.nelem >= SPG_BATCH_DIRECT_ELEMS &&
-            spg_plan_is_tma(b->dev, e.rank, e.dims, e.perm, e.factor, e.acc_factor, e.unsorted, e.sorted)) {
+        const int64_t own_min = g_own_min.load();
+        if (own_min > 0 && fo.nelem >= own_min &&
+            (g_own_any.load() ||
+             spg_plan_is_tma(b->dev, e.rank, e.dims, e.perm, e.factor, e.acc_factor, e.unsorted, e.sorted))) {
             const int op = spg_choose_op(e.factor, e.acc_factor);
             b->direct.push_back(i);
             b->bytes += fo.nelem * (spg_op_class(op) == 0 ? 16 : 24);

@@ -209,6 +209,8 @@ int *spg_status_word();
 // Whether the single-sort plan of a problem is the TMA-staged kernel (api.cu).
 bool spg_plan_is_tma(int dev, int rank, const int *dims, const int *perm, double factor, double acc_factor,
                      const double *unsorted, const double *sorted);
+// The batch options SPAGHETTY_OPT_BATCH_OWN_MIN / _OWN_KINDS (batch.cu).
+int spg_batch_option(int option, int value);
 // Asynchronous sort of device pointers of device `dev` (api.cu), no pointer checks.
 int spg_sort_async_on(int dev, int rank, const double *unsorted, double *sorted, const int *dims,
                       const int *perm, double factor, double acc_factor, void *stream);

@@ -255,3 +255,22 @@ def test_tma_candidates_replay_rank6():
     finally:
         clear()
     assert tried > 0
+
+
+def test_batch_own_launch_options():
+    """SPAGHETTY_OPT_BATCH_OWN_MIN takes element counts >= 0 (0: every sort
+    stays on the persistent kernel's work list); SPAGHETTY_OPT_BATCH_OWN_KINDS
+    takes 0 or 1.  Other values are rejected and leave the setting alone."""
+    L = lib()
+    own_min, own_kinds = 5, 6
+    try:
+        assert L.spaghetty_set_option(own_min, -1) == 9          # SPAGHETTY_ERR_CONFIG
+        assert L.spaghetty_set_option(own_kinds, 2) == 9
+        assert L.spaghetty_set_option(own_kinds, -1) == 9
+        assert L.spaghetty_set_option(own_min, 0) == 0
+        assert L.spaghetty_set_option(own_min, 1 << 20) == 0
+        assert L.spaghetty_set_option(own_kinds, 1) == 0
+        assert L.spaghetty_set_option(99, 0) == 9
+    finally:
+        L.spaghetty_set_option(own_min, 1 << 24)
+        L.spaghetty_set_option(own_kinds, 0)

@@ -9,6 +9,7 @@ import pytest
 
 from oracle import oracle as O
 from spaghetty_gb300 import plan
+from spaghetty_gb300._lib import lib
 from spaghetty_gb300.workloads import batched_mix
 from tests._util import bits_equal, first_mismatch
 
@@ -186,12 +187,26 @@ def test_size_bucket_rules(cuda, rule):
         assert bits_equal(got, want), (sp, rule, first_mismatch(got, want))
 
 
+OPT_BATCH_OWN_MIN = 5
+OWN_MIN_DEFAULT = 1 << 24
+
+
 def test_large_sorts_run_as_their_own_launches(cuda):
-    """Large sorts (2^22 elements and more) that the single-sort planner
-    puts on the TMA-staged kernel leave the work list and run as their own
-    launches inside the same launch (and the same captured graph); every
-    sort still matches the oracle."""
+    """Large sorts (SPAGHETTY_OPT_BATCH_OWN_MIN = 2^22 elements and more
+    here) that the single-sort planner puts on the TMA-staged kernel leave
+    the work list and run as their own launches inside the same launch (and
+    the same captured graph); every sort still matches the oracle.  At the
+    default threshold (2^24) the same sorts stay on the work list."""
     from spaghetty_gb300.batched import Batch
+    L = lib()
+    assert L.spaghetty_set_option(OPT_BATCH_OWN_MIN, 1 << 22) == 0
+    try:
+        _own_launches(cuda, Batch)
+    finally:
+        L.spaghetty_set_option(OPT_BATCH_OWN_MIN, OWN_MIN_DEFAULT)
+
+
+def _own_launches(cuda, Batch):
     specs = small_specs(40, 9)
     big = [{"dims": (64, 40, 40, 48), "perm": (2, 4, 3, 1), "factor": -0.5, "g": 0.0},
            {"dims": (16, 12, 12, 16, 8, 16), "perm": (6, 5, 4, 3, 2, 1), "factor": 1.0, "g": 1.0},
@@ -208,6 +223,11 @@ def test_large_sorts_run_as_their_own_launches(cuda):
               plan(sp["dims"], sp["perm"], opclass.get(sp["g"], 2))["kind"] == "tma"]
     assert len(direct) == 3 and big[3] not in direct
     assert info["jobs"] == 44 - len(direct) and info["launches"] == len(direct) + 1
+    lib().spaghetty_set_option(OPT_BATCH_OWN_MIN, OWN_MIN_DEFAULT)
+    dflt = Batch(jobs)              # planned only: nothing above 2^24 elements
+    assert dflt.info()["jobs"] == 44 and dflt.info()["launches"] == 1
+    dflt.close()
+    lib().spaghetty_set_option(OPT_BATCH_OWN_MIN, 1 << 22)
     b.capture()          # warm-up launch, then capture
     b.replay()           # the sorts ran twice: sortaccs accumulate twice
     assert b.status() == 0
