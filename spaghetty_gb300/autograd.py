@@ -28,6 +28,26 @@ def inverse(perm: Sequence[int]) -> tuple:
     return tuple(inv)
 
 
+# (input shape, perms as given) -> (perms as int tuples, output shape,
+# inverse perms): checked and derived once per signature, since at small
+# sizes the host work of a step is most of its time
+_SIGS: dict = {}
+
+
+def _signature(shape: tuple, perms: tuple):
+    key = (shape, perms)
+    sig = _SIGS.get(key)
+    if sig is None:
+        norm = tuple(tuple(int(v) for v in p) for p in perms)
+        shapes = {permuted_shape(shape, p) for p in norm}
+        if len(shapes) != 1:
+            raise ValueError("every permuted shape must agree, got %s" % sorted(shapes))
+        if len(_SIGS) > 4096:
+            _SIGS.clear()
+        sig = _SIGS[key] = (norm, shapes.pop(), tuple(inverse(p) for p in norm))
+    return sig
+
+
 def _chain(x: torch.Tensor, perms, factors, out_shape) -> torch.Tensor:
     """sum_k f_k * permute_k(x) with the rounding of one sort and len-1
     sortaccs: one fused launch where the fused kernels take the rank."""
@@ -43,19 +63,17 @@ def _chain(x: torch.Tensor, perms, factors, out_shape) -> torch.Tensor:
 class PermuteSum(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, perms, factors):
-        perms = tuple(tuple(int(v) for v in p) for p in perms)
+        in_shape = tuple(x.shape)
+        perms, out_shape, inv = _signature(in_shape, tuple(tuple(p) for p in perms))
         factors = tuple(float(f) for f in factors)
-        shapes = {permuted_shape(x.shape, p) for p in perms}
-        if len(shapes) != 1:
-            raise ValueError("every permuted shape must agree, got %s" % sorted(shapes))
-        ctx.perms = perms
+        ctx.inv = inv
         ctx.factors = factors
-        ctx.in_shape = tuple(x.shape)
-        return _chain(x, perms, factors, shapes.pop())
+        ctx.in_shape = in_shape
+        return _chain(x, perms, factors, out_shape)
 
     @staticmethod
     def backward(ctx, dy):
-        dx = _chain(dy.contiguous(), [inverse(p) for p in ctx.perms], ctx.factors, ctx.in_shape)
+        dx = _chain(dy.contiguous(), ctx.inv, ctx.factors, ctx.in_shape)
         return dx, None, None
 
 

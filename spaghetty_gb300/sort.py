@@ -177,31 +177,55 @@ __all__ = ["tce_sort_2", "tce_sortacc_2", "tce_sort_4", "tce_sortacc_4", "tce_so
            "plan", "permuted_shape", "SpaghettyError"]
 
 
+# (source shapes, perms, output shape) of fused calls seen so far ->
+# (rank, dims array, perms array): validated and built once, since at small
+# sizes a fused call's host time is mostly this bookkeeping
+_FUSED: dict = {}
+
+
+def _fused_arrays(shapes, perms, out_shape):
+    key = (shapes, perms, out_shape)
+    ent = _FUSED.get(key)
+    if ent is not None:
+        return ent
+    rank = len(shapes[0])
+    dims, pp = [], []
+    for shp, p in zip(shapes, perms):
+        if len(shp) != rank or len(p) != rank:
+            raise ValueError("every source must have the output's rank")
+        if permuted_shape(shp, p) != out_shape:
+            raise ValueError("permuted source shape %s != output shape %s"
+                             % (permuted_shape(shp, p), out_shape))
+        dims += [int(d) for d in shp]
+        pp += [int(v) for v in p]
+    if len(_FUSED) > 4096:
+        _FUSED.clear()
+    ent = _FUSED[key] = (rank, int_array(dims), int_array(pp))
+    return ent
+
+
+def _check_fp64_cuda(t, what):
+    if t.dtype != torch.float64 or not t.is_contiguous() or not t.is_cuda:
+        raise TypeError("%s must be contiguous CUDA FP64 tensors" % what)
+
+
 def _fused(entry, out, sources, perms, factors, stream):
-    from ._lib import int_array
     n = len(sources)
     if not (len(perms) == n == len(factors)) or n == 0:
         raise ValueError("sources, perms and factors must have one entry per term")
-    if out.dtype != torch.float64 or not out.is_contiguous() or not out.is_cuda:
-        raise TypeError("the output must be a contiguous CUDA FP64 tensor")
-    rank = sources[0].dim()
-    dims, pp, ptrs = [], [], []
-    for s, p in zip(sources, perms):
-        if s.dim() != rank or len(p) != rank:
-            raise ValueError("every source must have the output's rank")
-        if s.dtype != torch.float64 or not s.is_contiguous() or not s.is_cuda:
-            raise TypeError("sources must be contiguous CUDA FP64 tensors")
-        if permuted_shape(s.shape, p) != tuple(out.shape):
-            raise ValueError("permuted source shape %s != output shape %s"
-                             % (permuted_shape(s.shape, p), tuple(out.shape)))
-        dims += [int(d) for d in s.shape]
-        pp += [int(v) for v in p]
-        ptrs.append(s.data_ptr())
+    _check_fp64_cuda(out, "the output")
+    seen = None
+    for s in sources:
+        if s is not seen:
+            _check_fp64_cuda(s, "sources")
+            seen = s
+    rank, dims, pp = _fused_arrays(tuple(tuple(s.shape) for s in sources),
+                                   tuple(tuple(p) for p in perms), tuple(out.shape))
     if stream is None:
-        stream = torch.cuda.current_stream(out.device).cuda_stream
-    src_arr = (ctypes.c_void_p * n)(*ptrs)
+        stream = _raw_stream(out.device.index)
+    src_arr = (ctypes.c_void_p * n)(*[s.data_ptr() for s in sources])
     fac = (ctypes.c_double * n)(*[float(f) for f in factors])
-    rc = getattr(lib(), entry)(rank, n, src_arr, int_array(dims), int_array(pp), fac,
+    rc = getattr(lib(), entry)(rank, n, src_arr, dims, pp, fac,
                                ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(int(stream)))
     check(rc, entry)
     return out
