@@ -88,6 +88,25 @@ static inline size_t batch_smem_bytes(int stage_elems) {
 // dynamic bytes the launch needs the opt-in attribute.
 #define SPG_BATCH_SMEM_OPTIN (40 * 1024)
 
+// Elements of a thread's SPG_BATCH_EPT per box whose arbitrary-factor
+// product takes the 32-bit integer multiply (spg_mul: the same bits as the
+// rounded multiply) instead of the FP64 pipe, the busiest unit of this
+// kernel on random factors.  Measured on the batched configuration's mix
+// (GB/s): 0 4268, 1 4278, 2 4224, 4 3805 -- the kernel is bound by latency
+// (its block barrier per box, global and shared memory), not by the FP64
+// pipe, and the integer multiply's 40 instructions and registers cost more
+// than the FP64 cycles they free; so 0.
+#ifndef SPG_BATCH_INT_ELEMS
+#define SPG_BATCH_INT_ELEMS 0
+#endif
+
+template <int OP>
+__device__ __forceinline__ double spg_batch_apply(int k, double x, double y, const SpgFactor &F) {
+    if ((OP == OP_SORT_ANY || OP == OP_ACC_ANY) && k >= SPG_BATCH_EPT - SPG_BATCH_INT_ELEMS)
+        return spg_apply_flat<OP>(x, y, F);
+    return spg_apply<OP>(x, y, F);
+}
+
 // Status word bits.
 #define SPG_ST_BAD_JOB 1
 #define SPG_ST_BAD_UNIT 2
@@ -171,7 +190,7 @@ __device__ __forceinline__ void spg_batch_tiled(const BatchJob &j, const SpgTab<
         for (int k = 0; k < SPG_BATCH_EPT; ++k) {
             if (spg_valid(tb.pks[k], limA, limB)) {
                 const double x = tile[tb.smr[k]];
-                spg_st_out(dst + tb.ooff[k], spg_apply<OP>(x, spg_reads_out<OP>::value ? y[k] : 0.0, fac));
+                spg_st_out(dst + tb.ooff[k], spg_batch_apply<OP>(k, x, spg_reads_out<OP>::value ? y[k] : 0.0, fac));
             }
         }
     }
@@ -200,7 +219,7 @@ __device__ __forceinline__ void spg_batch_direct_box(const BatchJob &j, const Sp
     }
 #pragma unroll
     for (int k = 0; k < SPG_BATCH_EPT; ++k)
-        if (spg_valid(tb.pkl[k], limA, limB)) spg_st_out(dst + tb.ooff[k], spg_apply<OP>(v[k], y[k], fac));
+        if (spg_valid(tb.pkl[k], limA, limB)) spg_st_out(dst + tb.ooff[k], spg_batch_apply<OP>(k, v[k], y[k], fac));
 }
 
 template <int OP>

@@ -906,7 +906,9 @@ static int fused_pass(int rank, int nsrc, const double *const *unsorted, const i
 // of the cp.async kernel instead.  first_sets: the first source's product
 // starts the sum (a sort followed by sortaccs); the first pass then does not
 // read the output.
+#ifndef SPG_FUSED_ONE_PASS
 #define SPG_FUSED_ONE_PASS (int64_t(1) << 22)
+#endif
 
 static int fused_entry(const char *name, int rank, int nsrc, const double *const *unsorted,
                        const int *dims, const int *perms, const double *factors, double *sorted,
