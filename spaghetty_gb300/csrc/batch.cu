@@ -27,8 +27,6 @@
 #include <mutex>
 #include <vector>
 
-#define SPG_BATCH_NT 256
-#define SPG_BATCH_EPT 4
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
 // Elements per work unit (consecutive boxes of one sort, at most
 // SPG_BATCH_MAXB of them).  Each unit starts and drains its own cp.async

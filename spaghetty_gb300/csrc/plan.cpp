@@ -198,8 +198,8 @@ static const int kTRun = 32;      // minimum contiguous doubles per box row
 static const int kDirectRun = 16;  // shortest shared stride-1 row of the direct kernel
 static const int kVMax = 4096;    // largest box (512 threads x 8)
 static const int kDefaultStages = 3;
-static const int kBatchThreads = 256;
-static const int kBatchEpt = 4;
+static const int kBatchThreads = SPG_BATCH_NT;
+static const int kBatchEpt = SPG_BATCH_EPT;
 
 // Greedy box: grow the box until the input rows hold trun_in and the output
 // rows trun_out contiguous doubles (or the whole extent of that side), then

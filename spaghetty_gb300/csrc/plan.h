@@ -194,6 +194,14 @@ int spg_plan(const Folded &fo, int op, const int *box_override, int threads_over
 // `rank` whose largest extent lies in [ext_lo, ext_hi] get boxes grown until
 // the input and output rows hold run_in / run_out doubles, towards `volume`
 // elements.
+// CTA shape of the persistent batched kernel (batch.cu); its boxes hold at
+// most SPG_BATCH_NT * SPG_BATCH_EPT elements (spg_plan_batch).
+#ifndef SPG_BATCH_NT
+#define SPG_BATCH_NT 256
+#endif
+#ifndef SPG_BATCH_EPT
+#define SPG_BATCH_EPT 4
+#endif
 struct SpgBatchRule {
     int rank, ext_lo, ext_hi, run_in, run_out, volume;
 };
