@@ -497,9 +497,10 @@ int ccsd_t2_8_status(const double *a_raw, const int *size_a, const double *b_raw
  * loads it holds that array until exit); the caller passes only inputs and
  * outputs, and the call allocates nothing.  Limits: at most 1024 sorts, and
  * the work list must fit the 4 MiB: 896 bytes per sort plus 4 bytes per work
- * unit, a unit being up to 64 boxes and 64K elements of one sort (with 1024
- * sorts, about 819,000 units: some 53 G elements on 1024-element boxes, 13 G
- * on 256-element boxes); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The first
+ * unit, a unit being up to 64 boxes and 4K to 64K elements of one sort (the
+ * larger the batch, the longer its units; with 1024 sorts, about 819,000
+ * units: some 53 G elements on 1024-element boxes, 13 G on 256-element
+ * boxes); larger batches return SPAGHETTY_ERR_TOO_LARGE.  The first
  * call on a device looks up the array's device address (set-up); make that
  * first call before any stream capture.  Every call shares the one array,
  * which keeps the previous call's contents: the counter and status word are

@@ -29,12 +29,23 @@
 
 #define SPG_BATCH_VMAX (SPG_BATCH_NT * SPG_BATCH_EPT)
 // Elements per work unit (consecutive boxes of one sort, at most
-// SPG_BATCH_MAXB of them).  Each unit starts and drains its own cp.async
-// pipeline, so longer units leave fewer bubbles: on the batched
-// configuration's mix 16K -> 64K elements went from 4070 to 4235 GB/s (all
-// sorts on the work list); 48K and 96K measured 4218 and 4133.
+// SPG_BATCH_MAXB of them), a power of two from SPG_BATCH_UNIT_MIN to
+// SPG_BATCH_UNIT_ELEMS chosen per batch: the largest that still gives every
+// CTA SPG_BATCH_UNITS_PER_CTA units.  Each unit starts and drains its own
+// cp.async pipeline, so long units leave fewer bubbles (on the batched
+// configuration's mix 16K -> 64K elements went from 4070 to 4235 GB/s, all
+// sorts on the work list; 48K and 96K measured 4218 and 4133); but one CTA
+// moves a unit alone, at a few GB/s, so in a small batch the last long
+// units are its tail (the small-tile mix, 22M elements: 24.4M tiles/s with
+// 16K-element units, 20.8M with 64K).
 #ifndef SPG_BATCH_UNIT_ELEMS
 #define SPG_BATCH_UNIT_ELEMS 65536
+#endif
+#ifndef SPG_BATCH_UNIT_MIN
+#define SPG_BATCH_UNIT_MIN 4096
+#endif
+#ifndef SPG_BATCH_UNITS_PER_CTA
+#define SPG_BATCH_UNITS_PER_CTA 4
 #endif
 // Boxes per work unit at most: a unit's box offsets and edge limits are
 // computed once, one box per thread, into shared memory, so that the box
@@ -350,6 +361,24 @@ bool find_rule(int rank, const int *dims, SpgBatchRule *out) {
     return false;
 }
 
+// The work-unit size for a work list of `elems` elements on `dev`.
+int64_t batch_unit_elems(int64_t elems, int dev) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+        cudaGetLastError();
+        sms = 152;
+    }
+    const int64_t per = elems / ((int64_t)sms * SPG_BATCH_MINB * SPG_BATCH_UNITS_PER_CTA);
+    int64_t u = SPG_BATCH_UNIT_MIN;
+    while (u < SPG_BATCH_UNIT_ELEMS && 2 * u <= per) u *= 2;
+    return u;
+}
+
+// Boxes per work unit of a job whose boxes hold `vol` elements.
+uint32_t batch_chunk(int64_t unit_elems, int32_t vol) {
+    return (uint32_t)std::min<int64_t>(SPG_BATCH_MAXB, std::max<int64_t>(1, unit_elems / std::max(1, (int)vol)));
+}
+
 bool is_device_ptr(const void *p, int *dev) {
     cudaPointerAttributes at;
     std::memset(&at, 0, sizeof(at));
@@ -411,6 +440,7 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
     std::vector<uint32_t> unit_job;
     struct Range { uintptr_t lo, hi; int idx; bool out; };
     std::vector<Range> ranges;
+    int64_t list_elems = 0;                   // elements of the sorts on the work list
     int rc = SPAGHETTY_OK;
     for (int i = 0; i < n && rc == SPAGHETTY_OK; ++i) {
         const spaghetty_batch_entry &e = entries[i];
@@ -452,15 +482,21 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
         j.out = e.sorted;
         j.kind = pl.kind;
         j.op = op;
-        j.chunk = (uint32_t)std::min(SPG_BATCH_MAXB, std::max(1, SPG_BATCH_UNIT_ELEMS / std::max(1, (int)pl.kp.vol)));
-        j.ubeg = (uint32_t)unit_job.size();
-        const uint32_t units = (pl.kp.ntiles + j.chunk - 1) / j.chunk;
-        if ((uint64_t)unit_job.size() + units > 0xFFFFFFF0ull) { rc = SPAGHETTY_ERR_OVERFLOW; break; }
-        for (uint32_t q = 0; q < units; ++q) unit_job.push_back((uint32_t)b->jobs.size());
         if (pl.kind == KIND_TILED)
             b->smem_elems = std::max(b->smem_elems, (int)pl.kp.stage);
         b->bytes += fo.nelem * (spg_op_class(op) == 0 ? 16 : 24);
+        list_elems += fo.nelem;
         b->jobs.push_back(j);
+    }
+    // the work units, once the work list's size is known
+    const int64_t unit_elems = batch_unit_elems(list_elems, b->dev);
+    for (size_t q = 0; q < b->jobs.size() && rc == SPAGHETTY_OK; ++q) {
+        BatchJob &j = b->jobs[q];
+        j.chunk = batch_chunk(unit_elems, j.kp.vol);
+        j.ubeg = (uint32_t)unit_job.size();
+        const uint32_t units = (j.kp.ntiles + j.chunk - 1) / j.chunk;
+        if ((uint64_t)unit_job.size() + units > 0xFFFFFFF0ull) { rc = SPAGHETTY_ERR_OVERFLOW; break; }
+        for (uint32_t u = 0; u < units; ++u) unit_job.push_back((uint32_t)q);
     }
     if (rc == SPAGHETTY_OK) {
         // No output may overlap any other buffer of the batch (inputs may be
@@ -751,6 +787,7 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
     unsigned char *dbase = g_na_dev[dev];
     BatchJob *hjobs = reinterpret_cast<BatchJob *>(g_na_host + SPG_NOALLOC_JOBS_OFFSET);
     uint32_t njobs = 0, nunits = 0, nouts = 0;
+    int64_t list_elems = 0;
     int smem_elems = 2;
     // pass 1: validate and plan every sort into the host image
     for (int i = 0; i < n; ++i) {
@@ -783,13 +820,22 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
         j.out = e.sorted;
         j.kind = pl.kind;
         j.op = op;
-        j.chunk = (uint32_t)std::min(SPG_BATCH_MAXB, std::max(1, SPG_BATCH_UNIT_ELEMS / std::max(1, (int)pl.kp.vol)));
-        j.ubeg = nunits;
-        nunits += (pl.kp.ntiles + j.chunk - 1) / j.chunk;
         if (pl.kind == KIND_TILED)
             smem_elems = std::max(smem_elems, (int)pl.kp.stage);
+        list_elems += fo.nelem;
         ++njobs;
     }
+    // the work units, once the work list's size is known
+    const int64_t unit_elems = batch_unit_elems(list_elems, dev);
+    uint64_t units_all = 0;
+    for (uint32_t q = 0; q < njobs; ++q) {
+        BatchJob &j = hjobs[q];
+        j.chunk = batch_chunk(unit_elems, j.kp.vol);
+        j.ubeg = (uint32_t)units_all;
+        units_all += (j.kp.ntiles + j.chunk - 1) / j.chunk;
+        if (units_all > SPG_NOALLOC_BYTES / sizeof(uint32_t)) return SPAGHETTY_ERR_TOO_LARGE;
+    }
+    nunits = (uint32_t)units_all;
     // the unit map follows the job records
     const size_t units_off = (SPG_NOALLOC_JOBS_OFFSET + (size_t)njobs * sizeof(BatchJob) + 255) & ~(size_t)255;
     const size_t used = units_off + (size_t)nunits * sizeof(uint32_t);

@@ -235,3 +235,40 @@ def _own_launches(cuda, Batch):
         got = ds.cpu().numpy()
         want = expect(sp, u, y, g, times=2)
         assert bits_equal(got, want), (sp, first_mismatch(got, want))
+
+
+OPT_BATCH_OWN_KINDS = 6
+
+
+def test_own_launches_of_every_plan_kind(cuda):
+    """With SPAGHETTY_OPT_BATCH_OWN_KINDS = 1 the large sorts leave the work
+    list whatever their single-sort plan (here also an odd-extent sort on the
+    register-staged kernel and one that keeps its stride-1 index); the batch
+    still matches the oracle, replayed from a graph."""
+    from spaghetty_gb300.batched import Batch
+    L = lib()
+    specs = small_specs(24, 17)
+    big = [{"dims": (15, 17, 13, 11, 9, 13), "perm": (3, 2, 6, 1, 5, 4), "factor": 0.3, "g": 1.0},
+           {"dims": (40, 33, 21, 41), "perm": (3, 1, 2, 4), "factor": -1.0, "g": 0.0},
+           {"dims": (64, 40, 40, 48), "perm": (2, 4, 3, 1), "factor": 0.5, "g": 0.0}]
+    specs = specs[:12] + big + specs[12:]
+    jobs, host = make_jobs(specs, cuda, 500)
+    assert L.spaghetty_set_option(OPT_BATCH_OWN_MIN, 1 << 20) == 0
+    assert L.spaghetty_set_option(OPT_BATCH_OWN_KINDS, 1) == 0
+    try:
+        b = Batch(jobs)
+    finally:
+        L.spaghetty_set_option(OPT_BATCH_OWN_MIN, OWN_MIN_DEFAULT)
+        L.spaghetty_set_option(OPT_BATCH_OWN_KINDS, 0)
+    big_n = [sp for sp in specs if int(np.prod(sp["dims"])) >= 1 << 20]
+    info = b.info()
+    assert len(big_n) >= 3
+    assert info["jobs"] == len(specs) - len(big_n) and info["launches"] == len(big_n) + 1
+    b.capture()
+    b.replay()
+    assert b.status() == 0
+    for sp, (du, ds, *_), (u, y, g) in zip(specs, jobs, host):
+        got = ds.cpu().numpy()
+        want = expect(sp, u, y, g, times=2)
+        assert bits_equal(got, want), (sp, first_mismatch(got, want))
+    b.close()
