@@ -5,7 +5,8 @@
 // branches/spaghetty2/ccsd_t_tce_sort_list.txt).  One launch per call pays the
 // launch gap and a grid tail every time.  Here the host plans every sort once
 // (spg_plan_batch: one CTA shape for all), cuts each sort's boxes into work
-// units of ~16K elements, and uploads the job records plus a unit -> job map.
+// units of 4K-64K elements (longer in larger batches), and uploads the job
+// records plus a unit -> job map.
 // The persistent kernel's CTAs take units from an atomic counter; a CTA
 // rebuilds its per-element tables only when it moves to another sort.  The
 // launch (a counter reset and one kernel) is capturable in a CUDA graph.
