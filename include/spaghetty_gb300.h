@@ -226,8 +226,11 @@ const char *spaghetty_error_string(int code);
  * Pageable host buffers are always staged. */
 #define SPAGHETTY_OPT_HOST_ZERO_COPY 1
 /* SPAGHETTY_OPT_HOST_PIPELINE (default 0): when both buffers are pinned
- * host memory, move them in slabs along the output's slowest index through
- * a two-stream upload / sort / download pipeline instead. */
+ * host memory, move them in slabs through a three-stream upload / sort /
+ * download pipeline on the copy engines instead (slabs of the output's
+ * slowest index, or of the input's, whichever leaves one side contiguous
+ * and the other in long rows; where neither does, the kernels work on the
+ * pinned buffers in place as by default). */
 #define SPAGHETTY_OPT_HOST_PIPELINE 2
 /* SPAGHETTY_OPT_TMA_SKEW (default 1): TMA-staged plans may rotate the
  * permute step's slot map to spread its shared-memory accesses over the

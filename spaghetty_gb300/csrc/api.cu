@@ -697,52 +697,94 @@ struct DeviceGuard {
     }
 };
 
-// Two library streams and two slab buffer pairs per device for the pipeline.
+// Library streams and slab buffer pairs per device for the pipeline.
+#define SPG_PIPE_N 3
 struct PipeRes {
-    cudaStream_t st[2] = {nullptr, nullptr};
-    double *in[2] = {nullptr, nullptr}, *out[2] = {nullptr, nullptr};
+    cudaStream_t st[SPG_PIPE_N] = {};
+    double *in[SPG_PIPE_N] = {}, *out[SPG_PIPE_N] = {};
     size_t cap = 0;
 };
 std::map<int, PipeRes> g_pipe;
 
-// Host buffers moved in slabs along the OUTPUT's slowest index: slab c of
-// the output needs the input elements whose index a = perm[0]-1 lies in the
-// slab's range -- for each of the `outer` combinations of the input indices
-// before a, one contiguous run of (slab width x inner) elements, i.e. one
-// pitched 2-D copy.  The slab is then a smaller sort of the same
-// permutation, and the output slab is contiguous.  Slab c+1's upload runs
-// while slab c is sorted and downloaded (the two copy directions overlap).
-// Returns SPAGHETTY_ERR_CONFIG when the copy rows would be too short to pay.
+// Host buffers moved in slabs along one index c: slab [c0, c0 + cn) of
+// index c is, in the input, `outer_in` rows of cn * inner_in contiguous
+// elements (pitch d_c * inner_in) and, in the output, `outer_out` rows of
+// cn * inner_out (pitch d_c * inner_out).  Each slab is gathered by a
+// pitched 2-D copy into a packed device buffer, sorted there as a smaller
+// sort of the same permutation (d_c -> cn), and scattered back by a pitched
+// 2-D copy (a sortacc's old output is gathered the same way first).  Slabs
+// rotate over SPG_PIPE_N streams, so the upload of one slab, the sort of
+// another and the download of a third overlap (the two copy directions run
+// on separate copy engines).  The index is the output's slowest (the
+// download is contiguous) when its upload rows hold 32 KB, else the input's
+// slowest (the upload is contiguous) when its download rows do: measured on
+// GB300 at 100^4, pitched copies on both sides, or rows of a few KB, ran at
+// 200-250 GB/s against 310 with one side contiguous.  SPAGHETTY_ERR_CONFIG
+// when neither qualifies.
 int sort_host_pipelined(int rank, const double *u, double *s, const int *dims, const int *perm,
                         double f, double g, int dev, int sms) {
-    const int a = perm[0] - 1;
-    int64_t n = 1, outer = 1, inner = 1;
+    int64_t n = 1;
     for (int q = 0; q < rank; ++q) n *= dims[q];
-    for (int q = 0; q < a; ++q) outer *= dims[q];
-    for (int q = a + 1; q < rank; ++q) inner *= dims[q];
-    const int64_t E = dims[a];
-    const int64_t slice = n / E;                       // output elements per index value
-    int64_t cs = std::max<int64_t>(1, ((int64_t)16 << 20) / (slice * 8));   // ~16 MB slabs
-    cs = std::min<int64_t>(cs, std::max<int64_t>(1, (E + 3) / 4));        // at least ~4 slabs
-    if (E < 2 || (outer > 1 && cs * inner * 8 < 4096)) return SPAGHETTY_ERR_CONFIG;
+    int qpos[SPG_MAXR];                                 // output position of each input index
+    for (int q = 0; q < rank; ++q) qpos[perm[q] - 1] = q;
+    // slabs of ~32 MB of output, widened until the pitched side's rows hold
+    // 32 KB, at most 256 MB, and at least ~4 of them
+    const int64_t slab_target = (int64_t)32 << 20, slab_max = (int64_t)256 << 20;
+    const int64_t row_min = 4096;                       // elements: 32 KB
+    auto slab_of = [&](int k, int64_t row_unit, int64_t *cs_out) {
+        const int64_t slice = n / dims[k];
+        int64_t cs = std::max<int64_t>(slab_target / (slice * 8), (row_min + row_unit - 1) / row_unit);
+        cs = std::min<int64_t>(cs, std::max<int64_t>(1, slab_max / (slice * 8)));
+        cs = std::max<int64_t>(1, std::min<int64_t>(cs, dims[k] / 4));
+        *cs_out = cs;
+        return cs * row_unit;
+    };
+    int c = -1;
+    int64_t best_cs = 0;
+    const int a = perm[0] - 1;                          // the output's slowest index
+    if (a != rank - 1 && dims[a] >= 4) {
+        int64_t inner_in = 1, cs = 0;
+        for (int q = a + 1; q < rank; ++q) inner_in *= dims[q];
+        if (slab_of(a, inner_in, &cs) >= row_min) {
+            c = a;
+            best_cs = cs;
+        }
+    }
+    if (c < 0 && qpos[0] != rank - 1 && dims[0] >= 4) {
+        int64_t inner_out = 1, cs = 0;
+        for (int q = qpos[0] + 1; q < rank; ++q) inner_out *= dims[perm[q] - 1];
+        if (slab_of(0, inner_out, &cs) >= row_min) {
+            c = 0;
+            best_cs = cs;
+        }
+    }
+    if (c < 0) return SPAGHETTY_ERR_CONFIG;
+    const int64_t E = dims[c], cs = best_cs;
+    int64_t outer_in = 1, inner_in = 1, outer_out = 1, inner_out = 1;
+    for (int q = 0; q < c; ++q) outer_in *= dims[q];
+    for (int q = c + 1; q < rank; ++q) inner_in *= dims[q];
+    for (int q = 0; q < qpos[c]; ++q) outer_out *= dims[perm[q] - 1];
+    for (int q = qpos[c] + 1; q < rank; ++q) inner_out *= dims[perm[q] - 1];
+    if (E * inner_in * 8 > ((int64_t)1 << 31) || E * inner_out * 8 > ((int64_t)1 << 31))
+        return SPAGHETTY_ERR_CONFIG;                  // pitches beyond what 2-D copies take
     const bool acc = g != 0.0;
     PipeRes &pr = g_pipe[dev];
-    const size_t need = (size_t)(cs * slice);
+    const size_t need = (size_t)(cs * (n / E));
     if (!pr.st[0]) {
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < SPG_PIPE_N; ++b)
             if (cudaStreamCreateWithFlags(&pr.st[b], cudaStreamNonBlocking) != cudaSuccess) {
                 cudaGetLastError();
                 return SPAGHETTY_ERR_CUDA;
             }
     }
     if (pr.cap < need) {
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < SPG_PIPE_N; ++b) {
             if (pr.in[b]) cudaFree(pr.in[b]);
             if (pr.out[b]) cudaFree(pr.out[b]);
             pr.in[b] = pr.out[b] = nullptr;
         }
         pr.cap = 0;
-        for (int b = 0; b < 2; ++b)
+        for (int b = 0; b < SPG_PIPE_N; ++b)
             if (cudaMalloc((void **)&pr.in[b], need * 8) != cudaSuccess ||
                 cudaMalloc((void **)&pr.out[b], need * 8) != cudaSuccess) {
                 cudaGetLastError();
@@ -753,26 +795,27 @@ int sort_host_pipelined(int rank, const double *u, double *s, const int *dims, c
     int sub[SPG_MAXR];
     for (int q = 0; q < rank; ++q) sub[q] = dims[q];
     int rc = SPAGHETTY_OK;
-    int c = 0;
-    for (int64_t c0 = 0; c0 < E && rc == SPAGHETTY_OK; c0 += cs, ++c) {
+    int k = 0;
+    for (int64_t c0 = 0; c0 < E && rc == SPAGHETTY_OK; c0 += cs, ++k) {
         const int64_t cn = std::min<int64_t>(cs, E - c0);
-        const int b = c & 1;
+        const int b = k % SPG_PIPE_N;
         cudaStream_t st = pr.st[b];
-        const size_t w = (size_t)(cn * inner * 8);
-        if (cudaMemcpy2DAsync(pr.in[b], w, u + c0 * inner, (size_t)(E * inner * 8), w, (size_t)outer,
+        const size_t wi = (size_t)(cn * inner_in * 8), wo = (size_t)(cn * inner_out * 8);
+        const size_t pi = (size_t)(E * inner_in * 8), po = (size_t)(E * inner_out * 8);
+        if (cudaMemcpy2DAsync(pr.in[b], wi, u + c0 * inner_in, pi, wi, (size_t)outer_in,
                               cudaMemcpyHostToDevice, st) != cudaSuccess) { rc = SPAGHETTY_ERR_CUDA; break; }
-        if (acc && cudaMemcpyAsync(pr.out[b], s + c0 * slice, (size_t)(cn * slice * 8),
-                                   cudaMemcpyHostToDevice, st) != cudaSuccess) { rc = SPAGHETTY_ERR_CUDA; break; }
-        sub[a] = (int)cn;
+        if (acc && cudaMemcpy2DAsync(pr.out[b], wo, s + c0 * inner_out, po, wo, (size_t)outer_out,
+                                     cudaMemcpyHostToDevice, st) != cudaSuccess) { rc = SPAGHETTY_ERR_CUDA; break; }
+        sub[c] = (int)cn;
         Plan pl;
         rc = make_plan(rank, sub, perm, f, g, sms, &pl, true);
         if (rc) break;
         rc = launch_plan(pl, pr.in[b], pr.out[b], st, dev);
         if (rc) break;
-        if (cudaMemcpyAsync(s + c0 * slice, pr.out[b], (size_t)(cn * slice * 8), cudaMemcpyDeviceToHost,
-                            st) != cudaSuccess) { rc = SPAGHETTY_ERR_CUDA; break; }
+        if (cudaMemcpy2DAsync(s + c0 * inner_out, po, pr.out[b], wo, wo, (size_t)outer_out,
+                              cudaMemcpyDeviceToHost, st) != cudaSuccess) { rc = SPAGHETTY_ERR_CUDA; break; }
     }
-    for (int b = 0; b < 2; ++b)
+    for (int b = 0; b < SPG_PIPE_N; ++b)
         if (cudaStreamSynchronize(pr.st[b]) != cudaSuccess) rc = SPAGHETTY_ERR_CUDA;
     if (rc == SPAGHETTY_ERR_CUDA) cudaGetLastError();
     return rc ? rc : take_device_status();

@@ -368,3 +368,28 @@ def test_forced_tma_variants_rank6(cuda):
     finally:
         clear()
     assert ran > 0
+
+
+def test_pipelined_host_slabs(cuda):
+    """Pinned host buffers moved in slabs through the copy/sort/copy
+    pipeline (three streams), against the oracle, sort and sortacc: slabs of
+    the output's slowest index with pitched uploads (2413), of the input's
+    slowest index with pitched downloads (3142), and a permutation that no
+    slab index serves, which falls back to the kernels working on the pinned
+    buffers in place (4321)."""
+    dims = (64, 96, 80, 48)
+    n = int(np.prod(dims))
+    u = O.fixture_values(n, 72)
+    y = O.fixture_values(n, 73)
+    pu = torch.from_numpy(u).pin_memory()
+    assert lib().spaghetty_set_option(2, 1) == 0
+    try:
+        for perm in [(4, 3, 2, 1), (2, 4, 1, 3), (3, 1, 4, 2)]:
+            for f, g in ((-0.5, 0.0), (0.75, 1.0)):
+                ps = torch.from_numpy(y).pin_memory()
+                call_dropin("tce_sortacc_4" if g else "tce_sort_4", pu.data_ptr(), ps.data_ptr(),
+                            dims, perm, f)
+                assert lib().spaghetty_last_error() == 0
+                check(ps.numpy(), O.np_sort(u, dims, perm, f, g, out=y), ("pipelined slabs", perm, g))
+    finally:
+        lib().spaghetty_set_option(2, 0)
