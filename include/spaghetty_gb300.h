@@ -431,6 +431,19 @@ int spaghetty_batch_destroy(spaghetty_batch *batch);
  * Returns a SPAGHETTY_* code. */
 int spaghetty_batch_tune_set(int rank, int ext_lo, int ext_hi, int run_in, int run_out, int volume);
 
+/* Host replay of a batch's plan, needing no GPU: plans the entries as
+ * spaghetty_batch_create puts sorts on the persistent kernel's work list
+ * (every sort, as with SPAGHETTY_OPT_BATCH_OWN_MIN = 0; the entries'
+ * pointers are not read), checks each job record as the kernel does and that
+ * its work units cover its boxes once each, and replays every box through
+ * the kernel's own index functions: every read, write and staging slot in
+ * bounds, and every output element written once, from the input element the
+ * permutation maps to it.  num_sms: the SM count the work-unit sizes follow
+ * (0: 152).  stats (4 int64, may be NULL): jobs, work units, boxes,
+ * elements.  Sorts up to 2^27 elements.  SPAGHETTY_ERR_CONFIG on a violation
+ * (and above that size), with spaghetty_batch_bad_index() naming the entry. */
+int spaghetty_batch_verify(const spaghetty_batch_entry *entries, int n, int num_sms, int64_t *stats);
+
 /* ---- a contraction with its sorts fused --------------------------------- */
 
 /* The TCE pattern sort -> DGEMM('T','N') -> sort in one kernel

@@ -109,6 +109,8 @@ PROTOTYPES = {
     "spaghetty_batch_poison": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "spaghetty_batch_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "spaghetty_batch_tune_set": (ctypes.c_int, [ctypes.c_int] * 6),
+    "spaghetty_batch_verify": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                              ctypes.POINTER(ctypes.c_int64)]),
     "spaghetty_batch_launches": (ctypes.c_int, [ctypes.c_void_p]),
     "spaghetty_sortacc_fused": (ctypes.c_int, [ctypes.c_int, ctypes.c_int,
                                                ctypes.POINTER(ctypes.c_void_p), c_int_p, c_int_p,

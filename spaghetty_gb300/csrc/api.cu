@@ -1031,6 +1031,92 @@ int spg_sort_async_on(int dev, int rank, const double *unsorted, double *sorted,
 }
 
 // ===========================================================================
+// Host replay of one launch's index arithmetic (the kernels' own spg_box /
+// spg_walk), moving element indices instead of values: every global read
+// and write inside the tensors, every staging-tile slot inside smem_elems,
+// and every output element written exactly once, from the input element the
+// permutation maps to it.  Kinds: direct (each element read and written by
+// one thread), tiled and warp (staged through a tile in input order, read
+// back in output order).  stats (may be NULL): reads, writes, boxes, tile
+// elements.  Tensors up to 2^27 elements; SPAGHETTY_ERR_CONFIG on any
+// violation (and above that size).
+int spg_replay_params(const KParams &kp, const Folded &fo, int kind, int64_t smem_elems, int64_t *stats) {
+    const int64_t n = fo.nelem;
+    if (n > ((int64_t)1 << 27)) return SPAGHETTY_ERR_CONFIG;
+    const int R = fo.rank;
+    int64_t istr[SPG_MAXR];
+    {
+        int64_t s = 1;
+        for (int d = R - 1; d >= 0; --d) { istr[d] = s; s *= fo.D[d]; }
+    }
+    std::vector<int64_t> got((size_t)n, -1);
+    std::vector<int64_t> sm((size_t)std::max<int64_t>(smem_elems, 1), -2);
+    int64_t reads = 0, writes = 0;
+    for (uint32_t t = 0; t < kp.ntiles; ++t) {
+        int64_t ib, ob;
+        uint32_t limA, limB;
+        spg_box(kp, t, ib, ob, limA, limB);
+        for (uint32_t e = 0; e < (uint32_t)kp.vol; ++e) {
+            int32_t a, b, lin;
+            uint32_t pk;
+            spg_walk(kp.ld, e, a, b, lin, pk);
+            const bool v = spg_valid(pk, limA, limB);
+            if (kind == KIND_DIRECT) {
+                if (!v) continue;
+                const int64_t src = ib + a, dst = ob + b;
+                if (src < 0 || src >= n || dst < 0 || dst >= n) return SPAGHETTY_ERR_CONFIG;
+                if (got[(size_t)dst] != -1) return SPAGHETTY_ERR_CONFIG;
+                got[(size_t)dst] = src;
+                ++reads; ++writes;
+            } else {
+                const int64_t w = (int64_t)e + (kp.pad ? (int64_t)e / kp.pad : 0);
+                if (w < 0 || w >= smem_elems) return SPAGHETTY_ERR_CONFIG;
+                if (v) {
+                    const int64_t src = ib + a;
+                    if (src < 0 || src >= n) return SPAGHETTY_ERR_CONFIG;
+                    sm[(size_t)w] = src;
+                    ++reads;
+                } else {
+                    sm[(size_t)w] = -3;
+                }
+            }
+        }
+        if (kind == KIND_TILED || kind == KIND_WARP) {
+            for (uint32_t e = 0; e < (uint32_t)kp.vol; ++e) {
+                int32_t a, b, lin;
+                uint32_t pk;
+                spg_walk(kp.st, e, a, b, lin, pk);
+                if (!spg_valid(pk, limA, limB)) continue;
+                const int64_t r = (int64_t)lin + (kp.pad ? (int64_t)lin / kp.pad : 0);
+                if (r < 0 || r >= smem_elems) return SPAGHETTY_ERR_CONFIG;
+                const int64_t dst = ob + a;
+                if (dst < 0 || dst >= n) return SPAGHETTY_ERR_CONFIG;
+                if (got[(size_t)dst] != -1 || sm[(size_t)r] < 0) return SPAGHETTY_ERR_CONFIG;
+                got[(size_t)dst] = sm[(size_t)r];
+                ++writes;
+            }
+        }
+    }
+    // every output element written once, from the input element the
+    // permutation maps to it
+    for (int64_t o = 0; o < n; ++o) {
+        int64_t rem = o, src = 0;
+        for (int q = R - 1; q >= 0; --q) {
+            const int64_t ext = fo.D[fo.P[q]];
+            src += (rem % ext) * istr[fo.P[q]];
+            rem /= ext;
+        }
+        if (got[(size_t)o] != src) return SPAGHETTY_ERR_CONFIG;
+    }
+    if (stats) {
+        stats[0] = reads;
+        stats[1] = writes;
+        stats[2] = kp.ntiles;
+        stats[3] = smem_elems;
+    }
+    return SPAGHETTY_OK;
+}
+
 extern "C" {
 
 int spaghetty_tune_load(const char *path) {
@@ -1269,90 +1355,15 @@ int spaghetty_plan_verify(int rank, const int *dims, const int *perm, int op, in
     if (stats) for (int q = 0; q < 4; ++q) stats[q] = 0;
     if (pl.kind == KIND_EMPTY || pl.kind == KIND_FLAT) return SPAGHETTY_OK;
     if (pl.kind == KIND_TMA) return verify_tma(pl, stats);
-    const KParams &kp = pl.kp;
-    const Folded &fo = pl.fo;
-    const int64_t n = fo.nelem;
-    if (n > ((int64_t)1 << 27)) return SPAGHETTY_ERR_CONFIG;
-    const int R = fo.rank;
-    int64_t istr[SPG_MAXR];
-    {
-        int64_t s = 1;
-        for (int d = R - 1; d >= 0; --d) { istr[d] = s; s *= fo.D[d]; }
-    }
-    std::vector<int64_t> got((size_t)n, -1);
     // one staging tile: the whole buffer of the register-staged kernel, one
     // stage of the pipelined kernel
     // (the warp-shuffle transpose's "tile" is the warp's registers, vol
     // elements in input order, with no padding)
-    const int64_t smem_elems = pl.kind == KIND_WARP ? (int64_t)kp.vol
-                               : pl.stages ? (int64_t)kp.stage
+    const int64_t smem_elems = pl.kind == KIND_WARP ? (int64_t)pl.kp.vol
+                               : pl.stages ? (int64_t)pl.kp.stage
                                            : pl.smem_bytes / (int64_t)sizeof(double);
-    if (pl.stages && (int64_t)pl.stages * kp.stage * 8 > pl.smem_bytes) return SPAGHETTY_ERR_CONFIG;
-    std::vector<int64_t> sm((size_t)std::max<int64_t>(smem_elems, 1), -2);
-    int64_t reads = 0, writes = 0;
-    for (uint32_t t = 0; t < kp.ntiles; ++t) {
-        int64_t ib, ob;
-        uint32_t limA, limB;
-        spg_box(kp, t, ib, ob, limA, limB);
-        for (uint32_t e = 0; e < (uint32_t)kp.vol; ++e) {
-            int32_t a, b, lin;
-            uint32_t pk;
-            spg_walk(kp.ld, e, a, b, lin, pk);
-            const bool v = spg_valid(pk, limA, limB);
-            if (pl.kind == KIND_DIRECT) {
-                if (!v) continue;
-                const int64_t src = ib + a, dst = ob + b;
-                if (src < 0 || src >= n || dst < 0 || dst >= n) return SPAGHETTY_ERR_CONFIG;
-                if (got[(size_t)dst] != -1) return SPAGHETTY_ERR_CONFIG;
-                got[(size_t)dst] = src;
-                ++reads; ++writes;
-            } else {
-                const int64_t w = (int64_t)e + (kp.pad ? (int64_t)e / kp.pad : 0);
-                if (w < 0 || w >= smem_elems) return SPAGHETTY_ERR_CONFIG;
-                if (v) {
-                    const int64_t src = ib + a;
-                    if (src < 0 || src >= n) return SPAGHETTY_ERR_CONFIG;
-                    sm[(size_t)w] = src;
-                    ++reads;
-                } else {
-                    sm[(size_t)w] = -3;
-                }
-            }
-        }
-        if (pl.kind == KIND_TILED || pl.kind == KIND_WARP) {
-            for (uint32_t e = 0; e < (uint32_t)kp.vol; ++e) {
-                int32_t a, b, lin;
-                uint32_t pk;
-                spg_walk(kp.st, e, a, b, lin, pk);
-                if (!spg_valid(pk, limA, limB)) continue;
-                const int64_t r = (int64_t)lin + (kp.pad ? (int64_t)lin / kp.pad : 0);
-                if (r < 0 || r >= smem_elems) return SPAGHETTY_ERR_CONFIG;
-                const int64_t dst = ob + a;
-                if (dst < 0 || dst >= n) return SPAGHETTY_ERR_CONFIG;
-                if (got[(size_t)dst] != -1 || sm[(size_t)r] < 0) return SPAGHETTY_ERR_CONFIG;
-                got[(size_t)dst] = sm[(size_t)r];
-                ++writes;
-            }
-        }
-    }
-    // every output element written once, from the input element the
-    // permutation maps to it
-    for (int64_t o = 0; o < n; ++o) {
-        int64_t rem = o, src = 0;
-        for (int q = R - 1; q >= 0; --q) {
-            const int64_t ext = fo.D[fo.P[q]];
-            src += (rem % ext) * istr[fo.P[q]];
-            rem /= ext;
-        }
-        if (got[(size_t)o] != src) return SPAGHETTY_ERR_CONFIG;
-    }
-    if (stats) {
-        stats[0] = reads;
-        stats[1] = writes;
-        stats[2] = kp.ntiles;
-        stats[3] = smem_elems;
-    }
-    return SPAGHETTY_OK;
+    if (pl.stages && (int64_t)pl.stages * pl.kp.stage * 8 > pl.smem_bytes) return SPAGHETTY_ERR_CONFIG;
+    return spg_replay_params(pl.kp, pl.fo, pl.kind, smem_elems, stats);
 }
 
 int spaghetty_tune_set(int rank, const int *dims, const int *perm, int op, const int *box,

@@ -117,6 +117,22 @@ __device__ __forceinline__ double spg_batch_apply(int k, double x, double y, con
     return spg_apply<OP>(x, y, F);
 }
 
+// The kernel's check of a job record before it runs any of its units (a
+// record that fails it is skipped and flagged in the status word);
+// spaghetty_batch_verify runs the same check on the host.
+__host__ __device__ __forceinline__ bool spg_batch_job_ok(const BatchJob &j, int smem_elems) {
+    const KParams &p = j.kp;
+    const int tile = p.vol + (p.pad > 0 ? p.vol / p.pad + 1 : 0);
+    // the stages: SPG_BATCH_S of the sort's stage size fit the dynamic
+    // shared memory (smem_elems per stage)
+    return (j.kind == KIND_TILED || j.kind == KIND_DIRECT) && j.op >= 0 && j.op < OP_COUNT &&
+           p.vol >= 1 && p.vol <= SPG_BATCH_VMAX && p.pad >= 0 && j.in != nullptr && j.out != nullptr &&
+           j.chunk >= 1 && j.chunk <= SPG_BATCH_MAXB && p.lenA <= 0xFFFF && p.lenB <= 0xFFFF &&
+           p.ntiles >= 1 && p.ld.n >= 0 && p.ld.n <= SPG_MAXR && p.st.n >= 0 && p.st.n <= SPG_MAXR &&
+           p.grid.n >= 0 && p.grid.n <= SPG_MAXR &&
+           (j.kind != KIND_TILED || (tile <= p.stage && p.stage <= smem_elems));
+}
+
 // Status word bits.
 #define SPG_ST_BAD_JOB 1
 #define SPG_ST_BAD_UNIT 2
@@ -271,18 +287,7 @@ spg_batched(const BatchJob *__restrict__ jobs, uint32_t njobs,
             for (uint32_t i = tid; i < sizeof(BatchJob) / 4; i += SPG_BATCH_NT) dst[i] = src[i];
             __syncthreads();
             if (tid == 0) {
-                const KParams &p = sj.kp;
-                const int tile = p.vol + (p.pad > 0 ? p.vol / p.pad + 1 : 0);
-                // the stages: SPG_BATCH_S of the sort's stage size fit the
-                // dynamic shared memory (smem_elems per stage)
-                bool ok = (sj.kind == KIND_TILED || sj.kind == KIND_DIRECT) && sj.op >= 0 &&
-                          sj.op < OP_COUNT && p.vol >= 1 && p.vol <= SPG_BATCH_VMAX &&
-                          p.pad >= 0 && sj.in != nullptr && sj.out != nullptr && sj.chunk >= 1 &&
-                          sj.chunk <= SPG_BATCH_MAXB && p.lenA <= 0xFFFF && p.lenB <= 0xFFFF &&
-                          p.ntiles >= 1 && p.ld.n >= 0 && p.ld.n <= SPG_MAXR && p.st.n >= 0 &&
-                          p.st.n <= SPG_MAXR && p.grid.n >= 0 && p.grid.n <= SPG_MAXR &&
-                          (sj.kind != KIND_TILED || (tile <= p.stage && p.stage <= smem_elems)) &&
-                          u >= sj.ubeg;
+                const bool ok = spg_batch_job_ok(sj, smem_elems) && u >= sj.ubeg;
                 s_ok = ok ? 1 : 0;
                 if (!ok) atomicOr(status, SPG_ST_BAD_JOB);
             }
@@ -362,22 +367,48 @@ bool find_rule(int rank, const int *dims, SpgBatchRule *out) {
     return false;
 }
 
-// The work-unit size for a work list of `elems` elements on `dev`.
+// The work-unit size for a work list of `elems` elements on `sms` SMs.
+int64_t batch_unit_elems_sms(int64_t elems, int sms) {
+    const int64_t per = elems / ((int64_t)std::max(sms, 1) * SPG_BATCH_MINB * SPG_BATCH_UNITS_PER_CTA);
+    int64_t u = SPG_BATCH_UNIT_MIN;
+    while (u < SPG_BATCH_UNIT_ELEMS && 2 * u <= per) u *= 2;
+    return u;
+}
+
+// ... on device `dev`.
 int64_t batch_unit_elems(int64_t elems, int dev) {
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
         cudaGetLastError();
         sms = 152;
     }
-    const int64_t per = elems / ((int64_t)sms * SPG_BATCH_MINB * SPG_BATCH_UNITS_PER_CTA);
-    int64_t u = SPG_BATCH_UNIT_MIN;
-    while (u < SPG_BATCH_UNIT_ELEMS && 2 * u <= per) u *= 2;
-    return u;
+    return batch_unit_elems_sms(elems, sms);
 }
 
 // Boxes per work unit of a job whose boxes hold `vol` elements.
 uint32_t batch_chunk(int64_t unit_elems, int32_t vol) {
     return (uint32_t)std::min<int64_t>(SPG_BATCH_MAXB, std::max<int64_t>(1, unit_elems / std::max(1, (int)vol)));
+}
+
+// One sort of a batch planned as a work-list job: every field of the record
+// but chunk and ubeg, which depend on the whole work list.  *pfo (may be
+// NULL) receives the folded problem the job's parameters describe.
+int batch_plan_job(const spaghetty_batch_entry &e, const Folded &fo, BatchJob *j, Folded *pfo) {
+    Plan pl;
+    const int op = spg_choose_op(e.factor, e.acc_factor);
+    SpgBatchRule rule;
+    const bool have_rule = find_rule(e.rank, e.dims, &rule);
+    int rc = spg_plan_batch(fo, op, have_rule ? &rule : nullptr, &pl);
+    if (!rc) rc = spg_build_params(&pl, e.factor, e.acc_factor);
+    if (rc) return rc;
+    std::memset(j, 0, sizeof(*j));
+    j->kp = pl.kp;
+    j->in = e.unsorted;
+    j->out = e.sorted;
+    j->kind = pl.kind;
+    j->op = op;
+    if (pfo) *pfo = pl.fo;
+    return SPAGHETTY_OK;
 }
 
 bool is_device_ptr(const void *p, int *dev) {
@@ -469,23 +500,12 @@ int spaghetty_batch_create(const spaghetty_batch_entry *entries, int n, spaghett
             b->bytes += fo.nelem * (spg_op_class(op) == 0 ? 16 : 24);
             continue;
         }
-        Plan pl;
-        const int op = spg_choose_op(e.factor, e.acc_factor);
-        SpgBatchRule rule;
-        const bool have_rule = find_rule(e.rank, e.dims, &rule);
-        rc = spg_plan_batch(fo, op, have_rule ? &rule : nullptr, &pl);
-        if (!rc) rc = spg_build_params(&pl, e.factor, e.acc_factor);
-        if (rc) { g_batch_bad_index = i; break; }
         BatchJob j;
-        std::memset(&j, 0, sizeof(j));
-        j.kp = pl.kp;
-        j.in = e.unsorted;
-        j.out = e.sorted;
-        j.kind = pl.kind;
-        j.op = op;
-        if (pl.kind == KIND_TILED)
-            b->smem_elems = std::max(b->smem_elems, (int)pl.kp.stage);
-        b->bytes += fo.nelem * (spg_op_class(op) == 0 ? 16 : 24);
+        rc = batch_plan_job(e, fo, &j, nullptr);
+        if (rc) { g_batch_bad_index = i; break; }
+        if (j.kind == KIND_TILED)
+            b->smem_elems = std::max(b->smem_elems, (int)j.kp.stage);
+        b->bytes += fo.nelem * (spg_op_class(j.op) == 0 ? 16 : 24);
         list_elems += fo.nelem;
         b->jobs.push_back(j);
     }
@@ -803,26 +823,15 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
             g_batch_bad_index = i;
             return SPAGHETTY_ERR_MEMSPACE;
         }
-        Plan pl;
-        const int op = spg_choose_op(e.factor, e.acc_factor);
-        SpgBatchRule rule;
-        const bool have_rule = find_rule(e.rank, e.dims, &rule);
-        rc = spg_plan_batch(fo, op, have_rule ? &rule : nullptr, &pl);
-        if (!rc) rc = spg_build_params(&pl, e.factor, e.acc_factor);
+        BatchJob &j = hjobs[njobs];
+        rc = batch_plan_job(e, fo, &j, nullptr);
         if (rc) { g_batch_bad_index = i; return rc; }
         const uintptr_t nb = (uintptr_t)fo.nelem * sizeof(double);
         g_na_outs[nouts] = {(uintptr_t)e.sorted, (uintptr_t)e.sorted + nb, i};
         g_na_ins[nouts] = {(uintptr_t)e.unsorted, (uintptr_t)e.unsorted + nb, i};
         ++nouts;
-        BatchJob &j = hjobs[njobs];
-        std::memset(&j, 0, sizeof(j));
-        j.kp = pl.kp;
-        j.in = e.unsorted;
-        j.out = e.sorted;
-        j.kind = pl.kind;
-        j.op = op;
-        if (pl.kind == KIND_TILED)
-            smem_elems = std::max(smem_elems, (int)pl.kp.stage);
+        if (j.kind == KIND_TILED)
+            smem_elems = std::max(smem_elems, (int)j.kp.stage);
         list_elems += fo.nelem;
         ++njobs;
     }
@@ -897,4 +906,73 @@ extern "C" int spaghetty_sort_batch_noalloc(const spaghetty_batch_entry *entries
         return SPAGHETTY_ERR_CUDA;
     }
     return g_na_status ? SPAGHETTY_ERR_DEVICE : SPAGHETTY_OK;
+}
+
+// ===========================================================================
+// Host replay of a batch's plan (no GPU needed).
+extern "C" int spaghetty_batch_verify(const spaghetty_batch_entry *entries, int n, int num_sms,
+                                      int64_t *stats) {
+    g_batch_bad_index = -1;
+    if (stats) for (int q = 0; q < 4; ++q) stats[q] = 0;
+    if (n < 0 || (n > 0 && !entries)) return SPAGHETTY_ERR_NULL;
+    spg_autoload_tune();                      // the same size-bucket rules as a launch
+    std::vector<BatchJob> jobs;
+    std::vector<Folded> fos;
+    std::vector<int> idx;
+    int64_t list_elems = 0;
+    int smem_elems = 2;
+    for (int i = 0; i < n; ++i) {
+        const spaghetty_batch_entry &e = entries[i];
+        Folded fo;
+        int rc = spg_fold(e.rank, e.dims, e.perm, &fo);
+        if (rc) { g_batch_bad_index = i; return rc; }
+        if (fo.empty) continue;
+        // the records are replayed, not run: stand-in buffer addresses
+        spaghetty_batch_entry ev = e;
+        ev.unsorted = reinterpret_cast<const double *>(uintptr_t(256));
+        ev.sorted = reinterpret_cast<double *>(uintptr_t(512));
+        BatchJob j;
+        Folded pfo;
+        rc = batch_plan_job(ev, fo, &j, &pfo);
+        if (rc) { g_batch_bad_index = i; return rc; }
+        if (j.kind == KIND_TILED) smem_elems = std::max(smem_elems, (int)j.kp.stage);
+        list_elems += fo.nelem;
+        jobs.push_back(j);
+        fos.push_back(pfo);
+        idx.push_back(i);
+    }
+    const int64_t unit_elems = batch_unit_elems_sms(list_elems, num_sms > 0 ? num_sms : 152);
+    int64_t units = 0, boxes = 0, elems = 0;
+    for (size_t q = 0; q < jobs.size(); ++q) {
+        BatchJob &j = jobs[q];
+        j.chunk = batch_chunk(unit_elems, j.kp.vol);
+        j.ubeg = (uint32_t)units;
+        const int64_t cnt = ((int64_t)j.kp.ntiles + j.chunk - 1) / j.chunk;
+        // the units [ubeg, ubeg + cnt) cover boxes [0, ntiles) once each:
+        // unit u runs boxes [(u - ubeg) * chunk, min(+chunk, ntiles))
+        const bool cover = cnt >= 1 && cnt * (int64_t)j.chunk >= (int64_t)j.kp.ntiles &&
+                           (cnt - 1) * (int64_t)j.chunk < (int64_t)j.kp.ntiles;
+        if (!cover || !spg_batch_job_ok(j, smem_elems) || units + cnt > 0xFFFFFFF0ll) {
+            g_batch_bad_index = idx[q];
+            return SPAGHETTY_ERR_CONFIG;
+        }
+        // the boxes, through the kernels' own index functions: the tiled
+        // path stages each box in one stage of kp.stage elements
+        const int rc = spg_replay_params(j.kp, fos[q], j.kind, j.kind == KIND_TILED ? (int64_t)j.kp.stage : 1,
+                                         nullptr);
+        if (rc) {
+            g_batch_bad_index = idx[q];
+            return rc;
+        }
+        units += cnt;
+        boxes += j.kp.ntiles;
+        elems += fos[q].nelem;
+    }
+    if (stats) {
+        stats[0] = (int64_t)jobs.size();
+        stats[1] = units;
+        stats[2] = boxes;
+        stats[3] = elems;
+    }
+    return SPAGHETTY_OK;
 }

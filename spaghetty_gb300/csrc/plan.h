@@ -217,6 +217,9 @@ int *spg_status_word();
 // Whether the single-sort plan of a problem is the TMA-staged kernel (api.cu).
 bool spg_plan_is_tma(int dev, int rank, const int *dims, const int *perm, double factor, double acc_factor,
                      const double *unsorted, const double *sorted);
+// Host replay of one launch's index arithmetic (api.cu): in-bounds reads,
+// writes and tile slots, and a bijection onto the permuted output.
+int spg_replay_params(const KParams &kp, const Folded &fo, int kind, int64_t smem_elems, int64_t *stats);
 // The batch options SPAGHETTY_OPT_BATCH_OWN_MIN / _OWN_KINDS (batch.cu).
 int spg_batch_option(int option, int value);
 // Asynchronous sort of device pointers of device `dev` (api.cu), no pointer checks.
