@@ -432,6 +432,14 @@ def run_e2e(args, cases, torch, L, int_array, ctypes, warm=3):
 _CPU_STATE = {}
 
 
+def ref_thread_count() -> int:
+    """Host threads the reference's nests run on: every host core, or
+    SPAGHETTY_REF_THREADS.  (A launcher such as torchrun starts its ranks
+    with OMP_NUM_THREADS=1; the reference runs in rank 0 alone and takes the
+    whole host.)"""
+    return int(os.environ.get("SPAGHETTY_REF_THREADS", os.cpu_count() or 1))
+
+
 def _cpu_setup():
     """Build/load the reference nests, pick the loop order of every
     (perm, size) -- from oracle/ref_loop_orders.json when it was tuned on a
@@ -446,6 +454,7 @@ def _cpu_setup():
         return _CPU_STATE
     if R.load() is None:
         return None
+    R.set_threads(ref_thread_count())
     rng = np.random.default_rng(3)
     table = TR.load()
     best = {}
@@ -485,13 +494,11 @@ def cpu_sweep_sample(budget_s: float, threads: int | None = None, start: int = 0
     of each perm and size), timed over a bounded sample of the sweep
     starting at case `start`.  Returns (GB/s, cores, description, next)."""
     from spaghetty_gb300.workloads import PERMS4, SORT4_DIMS, SORT4_FACTORS
-    if threads:
-        os.environ["OMP_NUM_THREADS"] = str(threads)
     st = _cpu_setup()
     if st is None:
         return None
     R, best, bufs = st["R"], st["best"], st["bufs"]
-    cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    cores = R.set_threads(threads or ref_thread_count())
     total_b, total_t, calls = 0, 0.0, 0
     # sizes interleaved, so that any bounded prefix weights the sizes as the
     # whole sweep does
@@ -528,6 +535,7 @@ def cpu_sort6_baseline(budget_s):
         from spaghetty_gb300.workloads import TRIPLES_SORT6
         if R.load() is None:
             return {"value": None, "unit": UNIT, "error": "reference nests unavailable"}
+        R.set_threads(ref_thread_count())
         dims = (16,) * 6
         n = 16 ** 6
         rng = np.random.default_rng(6)
@@ -546,7 +554,7 @@ def cpu_sort6_baseline(budget_s):
                 dt = time.perf_counter() - t0
                 if bt is None or dt < bt:
                     bt, best[perm] = dt, lo
-        cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+        cores = R.set_threads(ref_thread_count())
         total_b, total_t, calls = 0, 0.0, 0
         t_start = time.perf_counter()
         order = [(p, acc) for p in TRIPLES_SORT6 for acc in (False, True)]

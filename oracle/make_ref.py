@@ -113,7 +113,7 @@ def generate() -> None:
 
     # dispatch table (our own code): name lookup by perm and loop order
     with open(os.path.join(OUT, "ref_table.c"), "w") as fh:
-        fh.write("#include <string.h>\n#include <stddef.h>\n")
+        fh.write("#include <string.h>\n#include <stddef.h>\n#include <omp.h>\n")
         fh.write("typedef void (*ref4_fn)(const double*, double*, const int*, const int*, "
                  "const int*, const int*, const double*, const double*);\n")
         fh.write("typedef void (*ref6_fn)(const double*, double*, const int*, const int*, "
@@ -136,6 +136,10 @@ def generate() -> None:
                  " : (int)(sizeof T6 / sizeof T6[0]); }\n")
         fh.write("const char *ref_perm(int rank, int i) { return rank == 4 ? T4[i].perm : T6[i].perm; }\n")
         fh.write("const char *ref_loop(int rank, int i) { return rank == 4 ? T4[i].loop : T6[i].loop; }\n")
+        # the OpenMP thread count of the nests, whatever OMP_NUM_THREADS the
+        # process started with (a launcher may have set it to 1)
+        fh.write("void ref_set_threads(int n) { if (n > 0) omp_set_num_threads(n); }\n")
+        fh.write("int ref_threads(void) { return omp_get_max_threads(); }\n")
         fh.write("int ref_call(int rank, int i, const double *u, double *s, const int *d,"
                  " double f, double g) {\n"
                  "  if (rank == 4) { T4[i].fn(u, s, d, d+1, d+2, d+3, &f, &g); return 0; }\n"

@@ -37,6 +37,11 @@ def load(build: bool = True):
     L.ref_call.argtypes = [ctypes.c_int, ctypes.c_int, dp, dp,
                            ctypes.POINTER(ctypes.c_int), ctypes.c_double, ctypes.c_double]
     L.ref_call.restype = ctypes.c_int
+    if hasattr(L, "ref_set_threads"):
+        L.ref_set_threads.argtypes = [ctypes.c_int]
+        L.ref_set_threads.restype = None
+        L.ref_threads.argtypes = []
+        L.ref_threads.restype = ctypes.c_int
     idx = {}
     for rank in (4, 6):
         for i in range(L.ref_count(rank)):
@@ -74,3 +79,13 @@ def call(perm: Sequence[int], loop: str, u: np.ndarray, s: np.ndarray,
                     float(factor), float(acc_factor))
     if rc:
         raise ValueError("bad rank")
+
+
+def set_threads(n: int) -> int:
+    """Run the nests on n OpenMP threads (whatever OMP_NUM_THREADS said when
+    the process started); returns the count in force."""
+    L = load()
+    if L is None or not hasattr(L, "ref_set_threads"):
+        return int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    L.ref_set_threads(int(n))
+    return int(L.ref_threads())
