@@ -64,7 +64,8 @@ class Batch:
         return ctypes.c_void_p(int(stream))
 
     def launch(self, stream=None) -> None:
-        """Enqueue the batch: the large sorts the single-sort planner puts on
+        """Enqueue the batch: the large sorts (2^24 elements and more by
+        default, SPAGHETTY_OPT_BATCH_OWN_MIN) the single-sort planner puts on
         the TMA-staged kernel one launch each, every other sort in ONE
         persistent kernel launch."""
         check(lib().spaghetty_batch_launch(self._h, self._stream(stream)), "batch launch")
@@ -109,6 +110,28 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def verify_plan(specs: Sequence[dict], num_sms: int = 0) -> dict:
+    """Host replay of the work list a batch of these sorts would get
+    (spaghetty_batch_verify, no GPU needed): specs are dicts with "dims",
+    "perm", "factor" and "acc" (or "acc_factor").  Returns the counts of
+    jobs, work units, boxes and elements; raises SpaghettyError naming the
+    first entry whose plan fails a check."""
+    arr = (BatchEntry * max(1, len(specs)))()
+    for e, sp in zip(arr, specs):
+        e.rank = len(sp["dims"])
+        for q, d in enumerate(sp["dims"]):
+            e.dims[q] = int(d)
+        for q, v in enumerate(sp["perm"]):
+            e.perm[q] = int(v)
+        e.factor = float(sp.get("factor", 1.0))
+        e.acc_factor = float(sp.get("acc_factor", 1.0 if sp.get("acc") else 0.0))
+    st = (ctypes.c_int64 * 4)()
+    rc = lib().spaghetty_batch_verify(ctypes.cast(arr, ctypes.c_void_p), len(specs), int(num_sms), st)
+    if rc:
+        raise SpaghettyError(rc, "batch entry %d" % lib().spaghetty_batch_bad_index())
+    return {"jobs": st[0], "units": st[1], "boxes": st[2], "elements": st[3]}
 
 
 def partition(jobs: Sequence[dict], rank: int, world: int) -> list[int]:

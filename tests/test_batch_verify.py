@@ -98,3 +98,18 @@ def test_bad_entry_is_named():
     rc, _ = verify(mix)
     assert rc == 2                                  # SPAGHETTY_ERR_PERM
     assert lib().spaghetty_batch_bad_index() == 5
+
+
+def test_python_wrapper():
+    from spaghetty_gb300._lib import SpaghettyError
+    from spaghetty_gb300.batched import verify_plan
+    mix = batched_mix(32, seed=9, ext4=(4, 16), ext6=(3, 6))
+    st = verify_plan(mix)
+    assert st["jobs"] == 32 and st["elements"] == sum(int(np.prod(m["dims"])) for m in mix)
+    bad = list(mix)
+    bad[3] = dict(bad[3], dims=(0,) + tuple(bad[3]["dims"][1:]))
+    st = verify_plan(bad)                       # an empty tensor is not a job
+    assert st["jobs"] == 31
+    bad[4] = dict(bad[4], perm=(2,) * len(bad[4]["dims"]))
+    with pytest.raises(SpaghettyError):
+        verify_plan(bad)
