@@ -635,10 +635,11 @@ bool overlaps(const double *a, const double *b, int64_t n) {
 // over NVLink-C2C on GB300, both directions at once -- instead of being
 // staged with copies.  spaghetty_set_option(SPAGHETTY_OPT_HOST_ZERO_COPY, 0)
 // turns that off (staging for every host buffer).
-int g_zero_copy = 1;
+std::atomic<int> g_zero_copy{1};
 // Pinned host buffers on both sides may instead be moved in slabs through a
-// two-stream copy/kernel/copy pipeline (SPAGHETTY_OPT_HOST_PIPELINE).
-int g_pipeline = 0;
+// three-stream copy/sort/copy pipeline (SPAGHETTY_OPT_HOST_PIPELINE).  Both
+// flags are read by calls on any thread, hence atomic.
+std::atomic<int> g_pipeline{0};
 
 // Where a pointer lives.  0 = pageable host memory, 1 = memory a kernel on
 // `dev` may access (device or managed), 2 = pinned host memory (its mapped
