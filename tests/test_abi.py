@@ -274,3 +274,28 @@ def test_batch_own_launch_options():
     finally:
         L.spaghetty_set_option(own_min, 1 << 24)
         L.spaghetty_set_option(own_kinds, 0)
+
+
+@pytest.mark.parametrize("name", ["spaghetty_sort_fused", "spaghetty_sortacc_fused"])
+def test_fused_entry_validation(name):
+    """The fused entries check their arguments before any launch: rank
+    (1..6), term count (1..16), null arrays, permutations, and the memory
+    space of the buffers (device memory only; host arrays are refused)."""
+    fn = getattr(lib(), name)
+    dbl = ctypes.c_double
+    u = np.zeros(24)
+    s = np.zeros(24)
+    srcs = (ctypes.c_void_p * 2)(u.ctypes.data, u.ctypes.data)
+    dims = int_array([2, 3, 4] * 2)
+    perms = int_array([3, 2, 1, 1, 3, 2])
+    fac = (dbl * 2)(1.0, -0.5)
+    out = ctypes.c_void_p(s.ctypes.data)
+    assert fn(0, 2, srcs, dims, perms, fac, out, None) == 1           # SPAGHETTY_ERR_RANK
+    assert fn(7, 2, srcs, dims, perms, fac, out, None) == 1
+    assert fn(3, 0, srcs, dims, perms, fac, out, None) == 9           # SPAGHETTY_ERR_CONFIG
+    assert fn(3, 17, srcs, dims, perms, fac, out, None) == 9
+    assert fn(3, 2, None, dims, perms, fac, out, None) == 5           # SPAGHETTY_ERR_NULL
+    assert fn(3, 2, srcs, dims, int_array([3, 2, 4, 1, 3, 2]), fac, out, None) == 2   # ERR_PERM
+    assert fn(3, 2, srcs, int_array([2, 0, 4] * 2), perms, fac, out, None) == 0       # empty
+    assert fn(3, 2, srcs, dims, perms, fac, out, None) == 8           # host arrays: ERR_MEMSPACE
+    assert np.all(s == 0.0)
