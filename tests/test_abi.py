@@ -299,3 +299,39 @@ def test_fused_entry_validation(name):
     assert fn(3, 2, srcs, int_array([2, 0, 4] * 2), perms, fac, out, None) == 0       # empty
     assert fn(3, 2, srcs, dims, perms, fac, out, None) == 8           # host arrays: ERR_MEMSPACE
     assert np.all(s == 0.0)
+
+
+C_CALLER = r"""
+#include <stdio.h>
+#include "spaghetty_gb300.h"
+int main(void) {
+    int dims[4] = {30, 30, 30, 30}, perm[4] = {4, 3, 2, 1}, bad[4] = {1, 1, 2, 3}, two = 2;
+    spaghetty_plan_info info;
+    int64_t st[4];
+    double u[16] = {0}, s[16] = {0}, f = 1.0;
+    int rq = spaghetty_plan_query(4, dims, perm, 0, &info);
+    int rv = spaghetty_plan_verify(4, dims, perm, 1, 152, st);
+    int rs = tce_sort_4_status(u, s, &two, &two, &two, &two, &bad[0], &bad[1], &bad[2], &bad[3], &f);
+    printf("%d %d %d %d %s\n", rq, info.kind, rv, rs, spaghetty_version());
+    return (rq == SPAGHETTY_OK && rv == SPAGHETTY_OK && rs == SPAGHETTY_ERR_PERM) ? 0 : 1;
+}
+"""
+
+
+def test_c_program_links_and_calls_the_library(tmp_path):
+    """A C caller compiled against include/spaghetty_gb300.h and linked with
+    the shared library (as NWChem's link line does) plans, replays a plan and
+    gets the reference's bad-permutation status, with no GPU."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    src = tmp_path / "caller.c"
+    src.write_text(C_CALLER)
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(LIB_PATH)
+    subprocess.check_call(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), str(src), "-o", str(exe),
+                           "-L", libdir, "-lspaghetty_gb300", "-Wl,-rpath," + libdir])
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.split()[3] == "2" and "spaghetty_gb300" in r.stdout
